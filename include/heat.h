@@ -1,0 +1,168 @@
+/*
+ * heat.h -- C ABI of the GB300 (sm_103a) 3D variable-coefficient heat solver.
+ *
+ * The solver advances   du/dt = div(kappa grad u) + f   on a uniform grid with
+ * zero Dirichlet boundaries by explicit time steps.  Each step applies the
+ * 7-point update of the reference serial solver
+ *   OpenMP_Single_Source/heat3D_variable_coeff.c:174-181
+ *   u_new = u_old + rhs + factor * ( (kE+kC)(uE-uC) - (kC+kW)(uC-uW)
+ *                                  + (kN+kC)(uN-uC) - (kC+kS)(uC-uS)
+ *                                  + (kU+kC)(uU-uC) - (kC+kD)(uC-uD) )
+ * with factor = dt/h/h/2 (heat3D_variable_coeff.c:84) to every interior point.
+ *
+ * Layout everywhere in this header: k-j-i with i fastest, offset
+ * k*ny*nx + j*nx + i, exactly the reference's IDX() (1-openmp.c:28-29).
+ * x == i, y == j, z == k.  Boundary points (i,j,k at 0 or n-1) are never
+ * written and keep the values they were given (zero in every reference run).
+ *
+ * Every function returns an int status: HEAT_OK (0) or a negative HEAT_E*
+ * code; heat_strerror() turns it into text.  Nothing in the library calls
+ * exit() or abort(); the reference exits from CUDA_CHECK
+ * (3D_Heat_Benchmark/NVIDIA-H100/Source-Results/CUDA/1-cuda.cu:42-50), a
+ * caller that wants that behaviour checks the status and exits itself.
+ *
+ * Threading: a heat_ctx is not thread-safe; distinct contexts may be driven
+ * from distinct host threads.  All work of a context is ordered on one CUDA
+ * stream (its own, or the one passed in heat_desc.stream).
+ */
+#ifndef HEAT_H
+#define HEAT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define HEAT_OK        0
+#define HEAT_EINVAL   (-1)   /* bad argument: sizes, NULL pointers, dt      */
+#define HEAT_ENOMEM   (-2)   /* device or host allocation failed            */
+#define HEAT_ECUDA    (-3)   /* a CUDA runtime call failed                  */
+#define HEAT_ETIMEOUT (-4)   /* a bounded device-side wait ran out          */
+#define HEAT_EBUDGET  (-5)   /* request exceeds the HBM budget (server)     */
+#define HEAT_ENODEV   (-6)   /* no CUDA device, or not an sm_103 device     */
+#define HEAT_ESTATE   (-7)   /* call not valid in the context's state       */
+
+/* ---- precision forms ----------------------------------------------------- */
+#define HEAT_FP64   0  /* FP64 fields; default kernel family (see flags)     */
+#define HEAT_FP32C  1  /* FP32 u + BF16 Kahan carry, FP32 face coefficients  */
+
+/* ---- flags (heat_desc.flags) ------------------------------------------- */
+/* Reference operation order, no FMA contraction: results are bit-identical
+ * to heat3D_variable_coeff.c built with -ffp-contract=off (the reference's
+ * --fmad=false CUDA build, CUDA/Makefile:36-37).  Without this flag the
+ * FP64 form uses precomputed face coefficients and is held to <=1e-12
+ * relative error against the reference instead.                              */
+#define HEAT_BITEXACT   0x1u
+/* Force the one-thread-per-point kernel (debug / comparison only).           */
+#define HEAT_NAIVE      0x2u
+/* Use only the hardware FP64 pipe in the default FP64 form (no integer
+ * accumulation); for comparison runs.                                         */
+#define HEAT_HWFP64     0x4u
+
+typedef struct heat_ctx heat_ctx;
+
+/* Problem description.  The host arrays are read during heat_init only. */
+typedef struct heat_desc {
+  int nx, ny, nz;          /* points per axis, boundary included, each >= 3  */
+  double h;                /* grid spacing                                   */
+  double dt;               /* time step; factor = dt/h/h/2 inside            */
+  const double *kappa;     /* host, nz*ny*nx, conductivity at points         */
+  const double *u0;        /* host, nz*ny*nx, initial field (boundary kept)  */
+  const double *rhs;       /* host, nz*ny*nx, per-step source; NULL = none   */
+  int precision;           /* HEAT_FP64 | HEAT_FP32C                         */
+  unsigned flags;          /* HEAT_BITEXACT | HEAT_NAIVE | HEAT_HWFP64       */
+  void *stream;            /* cudaStream_t to use, or NULL for an own stream */
+} heat_desc;
+
+/* ---- the solver ABI ------------------------------------------------------ */
+
+/* Allocate device fields, copy kappa/u0/rhs in, precompute face coefficients.
+ * Replaces the reference's host init + cudaMalloc/cudaMemcpy block
+ * (1-cuda.cu:200-224, 1-openmp.c:153-179).                                   */
+int heat_init(heat_ctx **out, const heat_desc *d);
+
+/* Advance nsteps explicit steps (asynchronous on the context's stream).
+ * Replaces the body of the reference's time loop, one heat_update() per step
+ * plus the pointer swap (1-cuda.cu:238-250, 1-openmp.c:193-205).            */
+int heat_step(heat_ctx *c, int nsteps);
+
+/* Reference time-loop semantics: while (t < T) { step; t += dt; } with t an
+ * FP64 host accumulator starting at 0 (heat3D_variable_coeff.c:155-193).
+ * The step count is replicated on the host; *steps_out receives it.         */
+int heat_run(heat_ctx *c, double T, int *steps_out);
+
+/* L2 norm sqrt(sum u^2) and checksum sum u over all nz*ny*nx points of the
+ * current field (FP64, deterministic two-pass warp-shuffle reduction).
+ * No reference counterpart; rel-L2 follows compare.py:60 of the reference's
+ * verify pipeline.  Synchronises the context's stream.                      */
+int heat_norm(heat_ctx *c, double *l2, double *checksum);
+
+/* Copy the current field (the reference's u_old after the swap,
+ * 1-cuda.cu:264) to / from a host array of nz*ny*nx doubles, k-j-i.
+ * For HEAT_FP32C the FP32 value plus its carry is widened to FP64.          */
+int heat_get_field(heat_ctx *c, double *u_host);
+int heat_set_field(heat_ctx *c, const double *u_host);
+
+/* Wait for all work queued on the context's stream.                          */
+int heat_sync(heat_ctx *c);
+
+/* Steps taken so far and kernel launches issued so far by this context.     */
+int heat_stats(heat_ctx *c, long long *steps_done, long long *kernel_launches);
+
+/* Release device memory and the context's own stream.                        */
+int heat_destroy(heat_ctx *c);
+
+const char *heat_strerror(int status);
+
+/* ---- drop-in for the reference's per-step device call -------------------- */
+
+/* Same signature and meaning as the reference's
+ *   static void heat_update(double *u_new, const double *u_old,
+ *                           const double *rhs, const double *kappa,
+ *                           int nz, int ny, int nx, double factor,
+ *                           int device_id)
+ * (OpenMP_Single_Source/1-openmp.c:55-58; CUDA wrapper 1-cuda.cu:116-119):
+ * device pointers, k-j-i layout with row length nx, updates every interior
+ * point of u_new from u_old, never touches boundary points.  The result is
+ * bit-identical to the reference's --fmad=false build.  rhs may be NULL.
+ * Runs on the legacy default stream of device_id, as the reference's
+ * <<<grid, block>>> launch does; returns a status instead of exiting.      */
+int heat_update(double *u_new, const double *u_old, const double *rhs,
+                const double *kappa, int nz, int ny, int nx, double factor,
+                int device_id);
+
+/* heat_update on an explicit stream (cudaStream_t passed as void*).          */
+int heat_update_async(double *u_new, const double *u_old, const double *rhs,
+                      const double *kappa, int nz, int ny, int nx,
+                      double factor, void *stream);
+
+/* ---- host-side input generators ------------------------------------------ */
+
+/* The reference's own initial data (heat3D_variable_coeff.c:79-150,
+ * 1-openmp.c:103-106,153-163) for an n^3 grid: h = 1/(n-1),
+ * dt = h*h/(12*0.95), rhs = dt*(1+cos cos cos), kappa = 0.5+0.45 sin sin sin,
+ * u0 = sin sin sin inside and exactly 0 on the boundary.  Arrays are n^3.   */
+int heat_inputs_reference(int n, double *kappa, double *rhs, double *u0,
+                          double *h_out, double *dt_out);
+
+/* Synthetic inputs of the benchmark configurations (cfg 0..4, seeded):
+ *   0: kappa = exp(0.5 g), g ~ N(0,1) i.i.d.; u0 ~ U[0,1) inside
+ *   1: kappa = 1 + 0.9 sin(2 pi x) sin(4 pi y) cos(2 pi z);
+ *      u0 = Gaussian bump, sigma 0.05, centre ~ U[0.3,0.7]^3
+ *   2: kappa log-normal (sigma 1) smoothed by 3 passes of a 3^3 box filter;
+ *      u0 ~ U[0,1) inside
+ *   3, 4: as 0 (per-grid / per-request seeds)
+ * h = 1/(max(nx,ny,nz)-1); dt = 0.9 h^2 / (6 kappa_max).  u0 is 0 on the
+ * boundary.  Arrays are nz*ny*nx, k-j-i.                                     */
+int heat_inputs_config(int cfg, uint64_t seed, int nx, int ny, int nz,
+                       double *kappa, double *u0, double *h_out,
+                       double *dt_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HEAT_H */

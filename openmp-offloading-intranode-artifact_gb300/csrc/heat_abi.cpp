@@ -1,0 +1,338 @@
+// extern "C" solver ABI (include/heat.h): context lifetime, field transfer,
+// the time loop and the drop-in heat_update().  Host code only; the kernels
+// live in the heat_*.cu translation units.
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "heat_internal.h"
+
+namespace {
+
+thread_local char g_last_error[256] = "";
+
+int cuda_fail(cudaError_t e, const char *what) {
+  std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
+  return HEAT_ECUDA;
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+bool geom_ok(int nx, int ny, int nz) {
+  if (nx < 3 || ny < 3 || nz < 3) return false;
+  // Rows, planes and fields must be indexable with the kernels' int / size_t
+  // arithmetic: keep each axis and the row count within int range.
+  if ((long long)ny * nz > 0x7fffffffLL) return false;
+  if (nx > (1 << 28)) return false;
+  return true;
+}
+
+heat_geom make_geom(int nx, int ny, int nz) {
+  heat_geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.pitch = (nx + 3) & ~3;
+  g.plane = (size_t)g.pitch * ny;
+  g.elems = g.plane * nz;
+  return g;
+}
+
+template <class T>
+int dalloc(T **p, size_t count) {
+  *p = nullptr;
+  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    std::snprintf(g_last_error, sizeof g_last_error, "cudaMalloc of %zu bytes: %s",
+                  count * sizeof(T), cudaGetErrorString(e));
+    return HEAT_ENOMEM;
+  }
+  return HEAT_OK;
+}
+
+// Copy a dense host k-j-i array into the pitched device layout.
+int upload(double *dst, const double *src, const heat_geom &g, cudaStream_t st) {
+  CK(cudaMemcpy2DAsync(dst, (size_t)g.pitch * sizeof(double), src, (size_t)g.nx * sizeof(double),
+                       (size_t)g.nx * sizeof(double), (size_t)g.ny * g.nz,
+                       cudaMemcpyHostToDevice, st));
+  return HEAT_OK;
+}
+
+int download(double *dst, const double *src, const heat_geom &g, cudaStream_t st) {
+  CK(cudaMemcpy2DAsync(dst, (size_t)g.nx * sizeof(double), src, (size_t)g.pitch * sizeof(double),
+                       (size_t)g.nx * sizeof(double), (size_t)g.ny * g.nz,
+                       cudaMemcpyDeviceToHost, st));
+  return HEAT_OK;
+}
+
+void free_ctx(heat_ctx *c) {
+  if (!c) return;
+  void *ptrs[] = {c->u[0],   c->u[1],     c->rhs,      c->kappa,    c->ks[0],   c->ks[1],
+                  c->ks[2],  c->c0,       c->cf[0],    c->cf[1],    c->cf[2],   c->v[0],
+                  c->v[1],   c->carry[0], c->carry[1], c->fcf[0],   c->fcf[1],  c->fcf[2],
+                  c->frhs,   c->partials};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int launch_step(heat_ctx *c) {
+  const heat_geom &g = c->g;
+  double *uo = c->u[c->cur], *un = c->u[c->cur ^ 1];
+  cudaError_t e;
+  if (c->flags & HEAT_NAIVE)
+    e = heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, c->stream);
+  else if (c->flags & HEAT_BITEXACT)
+    e = heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, c->stream);
+  else
+    e = heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, c->stream,
+                          (c->flags & HEAT_HWFP64) != 0);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  c->launches += 1;
+  c->cur ^= 1;
+  c->steps_done += 1;
+  return HEAT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *heat_strerror(int status) {
+  switch (status) {
+    case HEAT_OK: return "ok";
+    case HEAT_EINVAL: return "invalid argument";
+    case HEAT_ENOMEM: return g_last_error[0] ? g_last_error : "out of memory";
+    case HEAT_ECUDA: return g_last_error[0] ? g_last_error : "CUDA error";
+    case HEAT_ETIMEOUT: return "device-side wait timed out";
+    case HEAT_EBUDGET: return "request exceeds the HBM budget";
+    case HEAT_ENODEV: return "no usable CUDA device";
+    case HEAT_ESTATE: return "call not valid in this state";
+    default: return "unknown status";
+  }
+}
+
+int heat_init(heat_ctx **out, const heat_desc *d) {
+  if (!out) return HEAT_EINVAL;
+  *out = nullptr;
+  if (!d || !d->kappa || !d->u0) return HEAT_EINVAL;
+  if (!geom_ok(d->nx, d->ny, d->nz)) return HEAT_EINVAL;
+  if (!(d->h > 0.0) || !(d->dt > 0.0) || !std::isfinite(d->h) || !std::isfinite(d->dt))
+    return HEAT_EINVAL;
+  if (d->precision != HEAT_FP64) return HEAT_EINVAL;  // FP32C added separately
+
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return HEAT_ENODEV;
+  }
+
+  heat_ctx *c = new (std::nothrow) heat_ctx();
+  if (!c) return HEAT_ENOMEM;
+  c->g = make_geom(d->nx, d->ny, d->nz);
+  c->h = d->h;
+  c->dt = d->dt;
+  c->factor = d->dt / d->h / d->h / 2.0;  // as heat3D_variable_coeff.c:84
+  c->precision = d->precision;
+  c->flags = d->flags;
+  cudaGetDevice(&c->device);
+  if (d->stream) {
+    c->stream = (cudaStream_t)d->stream;
+    c->own_stream = false;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete c;
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+    c->own_stream = true;
+  }
+
+  const heat_geom &g = c->g;
+  const size_t bytes = g.elems * sizeof(double);
+  int rc = HEAT_OK;
+  double *kap = nullptr;  // raw kappa on the device (kept only for the naive kernel)
+#define TRY(x)                 \
+  do {                         \
+    rc = (x);                  \
+    if (rc != HEAT_OK) goto fail; \
+  } while (0)
+  TRY(dalloc(&c->u[0], g.elems));
+  TRY(dalloc(&c->u[1], g.elems));
+  TRY(dalloc(&kap, g.elems));
+  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
+  c->n_partials = heat::kNormBlocks;
+  if (cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+    goto fail;
+  }
+  TRY(upload(c->u[0], d->u0, g, c->stream));
+  TRY(upload(kap, d->kappa, g, c->stream));
+  // u_new starts as a copy of u0, so its boundary holds the same values
+  // (the reference seeds both buffers from u0, 1-cuda.cu:219-222).
+  if (cudaMemcpyAsync(c->u[1], c->u[0], bytes, cudaMemcpyDeviceToDevice, c->stream) !=
+      cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemcpy u0");
+    goto fail;
+  }
+  if (d->rhs) {
+    TRY(dalloc(&c->rhs, g.elems));
+    if (cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+      goto fail;
+    }
+    TRY(upload(c->rhs, d->rhs, g, c->stream));
+  }
+  if (c->flags & HEAT_NAIVE) {
+    c->kappa = kap;
+    kap = nullptr;
+  } else if (c->flags & HEAT_BITEXACT) {
+    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->ks[a], g.elems));
+    {
+      cudaError_t e = heat::launch_face_sums(c->ks, kap, g, c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "face sums"); goto fail; }
+      c->launches += 1;
+    }
+  } else {
+    TRY(dalloc(&c->c0, g.elems));
+    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
+    {
+      cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "coefficients"); goto fail; }
+      c->launches += 1;
+    }
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "heat_init sync");
+    goto fail;
+  }
+  if (kap) cudaFree(kap);
+  *out = c;
+  return HEAT_OK;
+fail:
+  if (kap) cudaFree(kap);
+  free_ctx(c);
+  return rc;
+#undef TRY
+}
+
+int heat_step(heat_ctx *c, int nsteps) {
+  if (!c || nsteps < 0) return HEAT_EINVAL;
+  for (int s = 0; s < nsteps; ++s) {
+    int rc = launch_step(c);
+    if (rc != HEAT_OK) return rc;
+  }
+  return HEAT_OK;
+}
+
+int heat_run(heat_ctx *c, double T, int *steps_out) {
+  if (!c) return HEAT_EINVAL;
+  // Replicate the reference's host accumulation exactly
+  // (heat3D_variable_coeff.c:155-192): the count depends on the rounding of
+  // the running sum, not on T/dt.
+  double t = 0.0;
+  long long steps = 0;
+  while (t < T) {
+    ++steps;
+    t += c->dt;
+    if (steps > 0x7fffffffLL) return HEAT_EINVAL;
+  }
+  int rc = heat_step(c, (int)steps);
+  if (steps_out) *steps_out = (int)steps;
+  return rc;
+}
+
+int heat_norm(heat_ctx *c, double *l2, double *checksum) {
+  if (!c) return HEAT_EINVAL;
+  cudaError_t e = heat::launch_norm_f64(c->u[c->cur], c->g, c->partials, c->n_partials, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "norm launch");
+  c->launches += 2;
+  double r[2];
+  CK(cudaMemcpyAsync(r, c->partials + 2 * c->n_partials, sizeof r, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (checksum) *checksum = r[0];
+  if (l2) *l2 = std::sqrt(r[1]);
+  return HEAT_OK;
+}
+
+int heat_get_field(heat_ctx *c, double *u_host) {
+  if (!c || !u_host) return HEAT_EINVAL;
+  int rc = download(u_host, c->u[c->cur], c->g, c->stream);
+  if (rc != HEAT_OK) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return HEAT_OK;
+}
+
+int heat_set_field(heat_ctx *c, const double *u_host) {
+  if (!c || !u_host) return HEAT_EINVAL;
+  // Both buffers take the new field so the boundary stays consistent in
+  // whichever one the next step writes.
+  int rc = upload(c->u[c->cur], u_host, c->g, c->stream);
+  if (rc != HEAT_OK) return rc;
+  CK(cudaMemcpyAsync(c->u[c->cur ^ 1], c->u[c->cur], c->g.elems * sizeof(double),
+                     cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return HEAT_OK;
+}
+
+int heat_sync(heat_ctx *c) {
+  if (!c) return HEAT_EINVAL;
+  CK(cudaStreamSynchronize(c->stream));
+  return HEAT_OK;
+}
+
+int heat_stats(heat_ctx *c, long long *steps_done, long long *kernel_launches) {
+  if (!c) return HEAT_EINVAL;
+  if (steps_done) *steps_done = c->steps_done;
+  if (kernel_launches) *kernel_launches = c->launches;
+  return HEAT_OK;
+}
+
+int heat_destroy(heat_ctx *c) {
+  if (!c) return HEAT_EINVAL;
+  cudaStreamSynchronize(c->stream);
+  free_ctx(c);
+  return HEAT_OK;
+}
+
+int heat_update_async(double *u_new, const double *u_old, const double *rhs,
+                      const double *kappa, int nz, int ny, int nx, double factor,
+                      void *stream) {
+  if (!u_new || !u_old || !kappa || u_new == u_old) return HEAT_EINVAL;
+  if (!geom_ok(nx, ny, nz)) return HEAT_EINVAL;
+  heat_geom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nz = nz;
+  g.pitch = nx;  // the reference's dense layout, IDX() of 1-openmp.c:28-29
+  g.plane = (size_t)nx * ny;
+  g.elems = g.plane * nz;
+  cudaError_t e = heat::launch_exact_raw(u_new, u_old, rhs, kappa, g, factor,
+                                         (cudaStream_t)stream);
+  if (e != cudaSuccess) return cuda_fail(e, "heat_update launch");
+  return HEAT_OK;
+}
+
+int heat_update(double *u_new, const double *u_old, const double *rhs, const double *kappa,
+                int nz, int ny, int nx, double factor, int device_id) {
+  if (device_id >= 0) {
+    int cur = -1;
+    CK(cudaGetDevice(&cur));
+    if (cur != device_id) CK(cudaSetDevice(device_id));
+  }
+  return heat_update_async(u_new, u_old, rhs, kappa, nz, ny, nx, factor, (void *)cudaStreamLegacy);
+}
+
+}  // extern "C"

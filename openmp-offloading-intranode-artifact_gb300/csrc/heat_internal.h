@@ -1,0 +1,83 @@
+// Internal declarations shared by the translation units of libheat.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "heat.h"
+
+// Device layout of one field: nz planes of ny rows of `pitch` doubles
+// (pitch >= nx, a multiple of 4 so every row starts on a 32-byte boundary).
+// Padding columns hold zeros and are never read as data.
+struct heat_geom {
+  int nx, ny, nz;
+  int pitch;          // elements per row on the device
+  size_t plane;       // pitch * ny
+  size_t elems;       // plane * nz
+};
+
+struct heat_ctx {
+  heat_geom g;
+  double h, dt, factor;
+  int precision;
+  unsigned flags;
+  int device;
+  cudaStream_t stream;
+  bool own_stream;
+
+  // FP64 state: ping-pong fields; cur indexes the current (u_old) one.
+  double *u[2];
+  int cur;
+  double *rhs;              // NULL when the problem has no source term
+
+  // Per-form coefficient planes (only the ones the chosen kernel uses).
+  double *kappa;            // raw conductivity (naive kernel)
+  double *ks[3];            // face kappa sums kx, ky, kz (bit-exact kernel)
+  double *c0;               // centre weight 1 - sum of face weights (fast)
+  double *cf[3];            // face weights factor*(kappa_a+kappa_b) (fast)
+
+  // FP32C state.
+  float *v[2];              // FP32 fields
+  uint16_t *carry[2];       // BF16 Kahan carry planes
+  float *fcf[3];            // FP32 face weights
+  float *frhs;              // FP32 source (NULL when none)
+
+  // Norm scratch: per-block partial sums, then the final pair.
+  double *partials;
+  int n_partials;
+
+  long long steps_done;
+  long long launches;
+};
+
+// ---- kernel launchers (each returns cudaError_t of the launch) ----------
+namespace heat {
+
+constexpr int kNormBlocks = 152 * 4;   // partial-sum blocks of the norm pass
+
+// heat_fp64_exact.cu (compiled with --fmad=false)
+cudaError_t launch_exact_raw(double *u_new, const double *u_old, const double *rhs,
+                             const double *kappa, const heat_geom &g, double factor,
+                             cudaStream_t st);
+cudaError_t launch_exact_faces(double *u_new, const double *u_old, const double *rhs,
+                               double *const ks[3], const heat_geom &g, double factor,
+                               cudaStream_t st);
+cudaError_t launch_naive(double *u_new, const double *u_old, const double *rhs,
+                         const double *kappa, const heat_geom &g, double factor,
+                         cudaStream_t st);
+cudaError_t launch_face_sums(double *const ks[3], const double *kappa, const heat_geom &g,
+                             cudaStream_t st);
+
+// heat_fp64_fast.cu
+cudaError_t launch_fast_coeffs(double *c0, double *const cf[3], const double *kappa,
+                               const heat_geom &g, double factor, cudaStream_t st);
+cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
+                        const double *c0, double *const cf[3], const heat_geom &g,
+                        cudaStream_t st, bool hw_only);
+
+// heat_reduce.cu
+cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,
+                            int nblocks, cudaStream_t st);
+
+}  // namespace heat

@@ -1,0 +1,120 @@
+"""C ABI checks that need no GPU: the library loads, exports every symbol the
+header declares, rejects bad arguments before touching a device, and its
+host-side input generators behave as specified."""
+from __future__ import annotations
+
+import ctypes as C
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, bits_equal
+
+HEADERS = sorted((ROOT / "include").glob("*.h"))
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(heat_[a-z_0-9]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_the_solver_abi():
+    names = declared_functions()
+    for n in ("heat_init", "heat_step", "heat_run", "heat_norm", "heat_update", "heat_destroy"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(heat):
+    lib = heat.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(heat.LIB_PATH)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\sT\s(heat_[a-z_0-9]+)$", out, flags=re.M))
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    for n in declared_functions():
+        assert getattr(lib, n) is not None
+    assert set(declared_functions()) <= set(heat.SIGNATURES)
+
+
+def test_strerror_covers_codes(heat):
+    lib = heat.lib()
+    for code in range(0, -8, -1):
+        assert lib.heat_strerror(code)
+    assert lib.heat_strerror(-99) == b"unknown status"
+
+
+def test_init_rejects_bad_arguments_without_a_device(heat):
+    lib = heat.lib()
+    ctx = C.c_void_p()
+    assert lib.heat_init(None, None) == heat.HEAT_EINVAL
+    assert lib.heat_init(C.byref(ctx), None) == heat.HEAT_EINVAL
+    k = np.ones((4, 4, 4))
+    for nx, ny, nz, h, dt in [(2, 4, 4, 0.1, 0.01), (4, 4, 4, 0.0, 0.01), (4, 4, 4, 0.1, -1.0),
+                              (4, 4, 4, float("nan"), 0.01)]:
+        d = heat.HeatDesc(nx, ny, nz, h, dt, k.ctypes.data, k.ctypes.data, None, 0, 0, None)
+        assert lib.heat_init(C.byref(ctx), C.byref(d)) == heat.HEAT_EINVAL
+    d = heat.HeatDesc(4, 4, 4, 0.1, 0.01, None, k.ctypes.data, None, 0, 0, None)
+    assert lib.heat_init(C.byref(ctx), C.byref(d)) == heat.HEAT_EINVAL
+    assert lib.heat_step(None, 1) == heat.HEAT_EINVAL
+    assert lib.heat_destroy(None) == heat.HEAT_EINVAL
+    assert lib.heat_update(None, None, None, None, 4, 4, 4, 0.1, 0) in (heat.HEAT_EINVAL, heat.HEAT_ECUDA)
+
+
+def test_reference_inputs_match_oracle_generator(heat, oracle):
+    """The library's and the oracle build's copies of the generator agree."""
+    a = heat.inputs_reference(13)
+    b = oracle.inputs_reference(13)
+    for x, y in zip(a[:3], b[:3]):
+        assert bits_equal(x, y)
+    assert a[3:] == b[3:]
+
+
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
+def test_config_inputs_properties(heat, cfg):
+    nx, ny, nz = 13, 9, 11
+    kappa, u0, h, dt = heat.inputs_config(cfg, 7, nx, ny, nz)
+    assert kappa.shape == (nz, ny, nx)
+    assert h == 1.0 / (max(nx, ny, nz) - 1)
+    assert np.all(kappa > 0)
+    assert dt == pytest.approx(0.9 * h * h / (6 * kappa.max()), rel=1e-15)
+    b = np.ones_like(u0, dtype=bool)
+    b[1:-1, 1:-1, 1:-1] = False
+    assert np.all(u0[b] == 0.0)
+    assert np.all(u0[~b] >= 0.0) and np.all(u0[~b] < 1.0 + 1e-15)
+    k2, u2, _, _ = heat.inputs_config(cfg, 7, nx, ny, nz)
+    assert bits_equal(kappa, k2) and bits_equal(u0, u2)
+    k3, u3, _, _ = heat.inputs_config(cfg, 8, nx, ny, nz)
+    assert not bits_equal(u0, u3)
+
+
+def test_config0_distributions(heat):
+    kappa, u0, h, dt = heat.inputs_config(0, 1, 64, 64, 64)
+    g = np.log(kappa) / 0.5
+    assert abs(g.mean()) < 0.01 and abs(g.std() - 1.0) < 0.01
+    inner = u0[1:-1, 1:-1, 1:-1]
+    assert abs(inner.mean() - 0.5) < 0.01 and abs(inner.var() - 1 / 12) < 0.005
+
+
+def test_config1_fields(heat):
+    n = 33
+    kappa, u0, h, dt = heat.inputs_config(1, 5, n, n, n)
+    x = np.arange(n) * h
+    kk = 1 + 0.9 * np.sin(2 * np.pi * x)[None, None, :] * np.sin(4 * np.pi * x)[None, :, None] * \
+        np.cos(2 * np.pi * x)[:, None, None]
+    assert np.allclose(kappa, kk, rtol=0, atol=1e-14)
+    k, j, i = np.unravel_index(np.argmax(u0), u0.shape)
+    assert 0.25 <= i * h <= 0.75 and 0.25 <= j * h <= 0.75 and 0.25 <= k * h <= 0.75
+    assert u0.max() > 0.3
+
+
+def test_config2_kappa_is_smoothed(heat):
+    kappa, u0, h, dt = heat.inputs_config(2, 2, 24, 24, 24)
+    raw, _, _, _ = heat.inputs_config(0, 2, 24, 24, 24)
+    # smoothing shrinks the spread of log kappa well below sigma = 1
+    assert np.log(kappa).std() < 0.5
+    assert np.all(np.isfinite(kappa))

@@ -1,0 +1,217 @@
+"""GPU parity: libheat's FP64 kernels against the oracle and the golden
+fixtures, through the C ABI.
+
+Bars (written in the tests):
+  - HEAT_BITEXACT, HEAT_NAIVE and the heat_update() drop-in: bit-identical to
+    the reference serial / oracle;
+  - default FP64 form: max relative error <= 1e-12 (compare.py's max-rel,
+    |ref| > 1e-12) and rel-L2 <= 1e-13;
+  - norms: <= 1e-13 relative to the oracle's compensated sums.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import bits_equal, golden_cases, golden_npz, metrics
+
+pytestmark = pytest.mark.gpu
+
+FAST_MAX_REL = 1e-12
+FAST_REL_L2 = 1e-13
+
+
+@pytest.fixture(scope="module")
+def H(heat, cuda_device):
+    return heat
+
+
+def solve(H, kappa, u0, h, dt, steps=None, T=None, rhs=None, flags=0):
+    with H.Solver(kappa, u0, h, dt, rhs=rhs, flags=flags) as s:
+        n = s.run(T) if T is not None else (s.step(steps) or steps)
+        return s.field(), n, s.norm()
+
+
+FORMS = {"bitexact": 1, "naive": 1 | 2}
+
+
+@pytest.mark.parametrize("path", golden_npz(), ids=lambda p: p.stem)
+@pytest.mark.parametrize("form", ["bitexact", "naive", "default"])
+def test_golden_reference_problem(H, path, form):
+    z = np.load(path)
+    n, steps, h, dt, T = z["meta"]
+    flags = FORMS.get(form, 0)
+    u, s, _ = solve(H, z["kappa"], z["u0"], h, dt, T=T, rhs=z["rhs"], flags=flags)
+    assert s == int(steps)
+    if form == "default":
+        m = metrics(z["u"], u)
+        assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    else:
+        assert bits_equal(u, z["u"])
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if c["n"] >= 51], ids=lambda c: f"n{c['n']}")
+def test_reference_problem_larger(H, oracle, case):
+    """The reference's verify sizes (N=256/100 steps is verify.sh's default)."""
+    n = case["n"]
+    kappa, rhs, u0, h, dt = H.inputs_reference(n)
+    u_or, s_or = oracle.run_T(u0, kappa, h, dt, float(case["T"]), rhs=rhs)
+    assert s_or == case["steps"]
+    u_ex, s_ex, _ = solve(H, kappa, u0, h, dt, T=float(case["T"]), rhs=rhs, flags=1)
+    assert s_ex == s_or
+    assert bits_equal(u_ex, u_or)
+    u_fa, _, _ = solve(H, kappa, u0, h, dt, T=float(case["T"]), rhs=rhs, flags=0)
+    m = metrics(u_or, u_fa)
+    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+
+
+SHAPES = [(3, 3, 3), (4, 5, 6), (5, 4, 3), (33, 17, 9), (31, 33, 35), (64, 8, 40), (130, 67, 21)]
+
+
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_odd_and_uneven_grids(H, oracle, shape):
+    nx, ny, nz = shape
+    kappa, u0, h, dt = H.inputs_config(0, 11, nx, ny, nz)
+    u_or = oracle.steps(u0, kappa, h, dt, 23)
+    for flags in (1, 3):
+        u, _, _ = solve(H, kappa, u0, h, dt, steps=23, flags=flags)
+        assert bits_equal(u, u_or), flags
+    u, _, _ = solve(H, kappa, u0, h, dt, steps=23, flags=0)
+    m = metrics(u_or, u)
+    assert m["max_rel"] <= FAST_MAX_REL, m
+
+
+def test_config0_full(H, oracle):
+    """128^3, kappa = exp(0.5 g), 100 steps (the reference-CPU-sized case)."""
+    kappa, u0, h, dt = H.inputs_config(0, 2026, 128, 128, 128)
+    u_or = oracle.steps(u0, kappa, h, dt, 100)
+    u_ex, _, (l2, cs) = solve(H, kappa, u0, h, dt, steps=100, flags=1)
+    assert bits_equal(u_ex, u_or)
+    l2_or, cs_or = oracle.norm(u_or)
+    assert l2 == pytest.approx(l2_or, rel=1e-13) and cs == pytest.approx(cs_or, rel=1e-13)
+    u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=100, flags=0)
+    m = metrics(u_or, u_fa)
+    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+
+
+def test_config1_reduced(H, oracle):
+    """Config-1 fields (smooth kappa, Gaussian bump) at 96^3, 300 steps."""
+    kappa, u0, h, dt = H.inputs_config(1, 7, 96, 96, 96)
+    u_or = oracle.steps(u0, kappa, h, dt, 300)
+    u_ex, _, _ = solve(H, kappa, u0, h, dt, steps=300, flags=1)
+    assert bits_equal(u_ex, u_or)
+    u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=300, flags=0)
+    m = metrics(u_or, u_fa)
+    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+
+
+def test_config1_full_size_short(H, oracle):
+    """512^3 (config-1 shape) for 8 steps against the oracle: bitwise and <=1e-12."""
+    kappa, u0, h, dt = H.inputs_config(1, 1, 512, 512, 512)
+    u_or = oracle.steps(u0, kappa, h, dt, 8)
+    u_ex, _, _ = solve(H, kappa, u0, h, dt, steps=8, flags=1)
+    assert bits_equal(u_ex, u_or)
+    del u_ex
+    u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=8, flags=0)
+    m = metrics(u_or, u_fa)
+    assert m["max_rel"] <= FAST_MAX_REL, m
+
+
+def test_config1_full_size_1000_steps_properties(H):
+    """Config 1 exactly (512^3, 1000 steps): the default form against the
+    bit-exact form on the GPU (the bit-exact form equals the oracle above),
+    and size-independent properties: zero boundary kept, maximum principle
+    (no new extrema without a source), heat leaves through the boundary."""
+    kappa, u0, h, dt = H.inputs_config(1, 1, 512, 512, 512)
+    u_ex, _, (l2e, cse) = solve(H, kappa, u0, h, dt, steps=1000, flags=1)
+    u_fa, _, (l2f, csf) = solve(H, kappa, u0, h, dt, steps=1000, flags=0)
+    m = metrics(u_ex, u_fa)
+    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    b = np.ones(u_fa.shape, dtype=bool)
+    b[1:-1, 1:-1, 1:-1] = False
+    assert np.all(u_fa[b] == 0.0)
+    assert u_fa.min() >= 0.0 and u_fa.max() <= u0.max() * (1 + 1e-12)
+    assert 0 < cse < float(u0.sum())
+    assert csf == pytest.approx(cse, rel=1e-12) and l2f == pytest.approx(l2e, rel=1e-12)
+
+
+def test_nonzero_boundary_is_never_written(H):
+    kappa, u0, h, dt = H.inputs_config(0, 4, 20, 18, 16)
+    rng = np.random.default_rng(0)
+    u0 = u0.copy()
+    b = np.ones(u0.shape, dtype=bool)
+    b[1:-1, 1:-1, 1:-1] = False
+    u0[b] = rng.uniform(1, 2, b.sum())
+    for flags in (0, 1, 3):
+        u, _, _ = solve(H, kappa, u0, h, dt, steps=17, flags=flags)
+        assert bits_equal(u[b], u0[b]), flags
+
+
+def test_run_T_matches_reference_count(H, oracle):
+    n = 40
+    kappa, rhs, u0, h, dt = H.inputs_reference(n)
+    for steps, fmt in ((77, "%.7g"), (50, "%.17g")):
+        T = oracle.verify_T(n, steps, fmt=fmt)
+        _, s, _ = solve(H, kappa, u0, h, dt, T=T, rhs=rhs, flags=1)
+        assert s == oracle.count_steps(T, dt)
+
+
+def test_norm_matches_oracle(H, oracle):
+    kappa, u0, h, dt = H.inputs_config(0, 9, 70, 45, 33)
+    with H.Solver(kappa, u0, h, dt) as s:
+        l2, cs = s.norm()
+        l2b, csb = s.norm()
+    l2o, cso = oracle.norm(u0)
+    assert l2 == pytest.approx(l2o, rel=1e-13) and cs == pytest.approx(cso, rel=1e-13)
+    assert (l2, cs) == (l2b, csb)
+
+
+def test_get_set_field_roundtrip(H):
+    kappa, u0, h, dt = H.inputs_config(0, 1, 21, 22, 23)
+    with H.Solver(kappa, u0, h, dt, flags=1) as s:
+        assert bits_equal(s.field(), u0)
+        s.step(3)
+        mid = s.field()
+        s.step(4)
+        end = s.field()
+        s.set_field(mid)
+        s.step(4)
+        assert bits_equal(s.field(), end)
+        steps, launches = s.stats()
+        assert steps == 11 and launches >= 11
+
+
+def test_heat_update_dropin(H, oracle, cuda_device):
+    """The reference's per-step call on raw device pointers, dense layout,
+    called exactly as 1-cuda.cu:241-246 does (swap in the caller)."""
+    torch = cuda_device
+    for n, steps in ((17, 9), (64, 25)):
+        kappa, rhs, u0, h, dt = H.inputs_reference(n)
+        factor = oracle.factor(h, dt)
+        d_old = torch.from_numpy(u0).cuda()
+        d_new = d_old.clone()
+        d_rhs = torch.from_numpy(rhs).cuda()
+        d_kap = torch.from_numpy(kappa).cuda()
+        for _ in range(steps):
+            H.check(H.lib().heat_update(d_new.data_ptr(), d_old.data_ptr(), d_rhs.data_ptr(),
+                                        d_kap.data_ptr(), n, n, n, factor, 0), "heat_update")
+            d_old, d_new = d_new, d_old
+        torch.cuda.synchronize()
+        u_or = oracle.steps(u0, kappa, h, dt, steps, rhs=rhs)
+        assert bits_equal(d_old.cpu().numpy(), u_or)
+
+
+def test_heat_update_dropin_uneven_no_rhs(H, oracle, cuda_device):
+    torch = cuda_device
+    nx, ny, nz = 37, 19, 11
+    kappa, u0, h, dt = H.inputs_config(0, 5, nx, ny, nz)
+    factor = oracle.factor(h, dt)
+    a = torch.from_numpy(u0).cuda()
+    b = a.clone()
+    k = torch.from_numpy(kappa).cuda()
+    for _ in range(6):
+        H.check(H.lib().heat_update(b.data_ptr(), a.data_ptr(), None, k.data_ptr(), nz, ny, nx,
+                                    factor, 0), "heat_update")
+        a, b = b, a
+    torch.cuda.synchronize()
+    assert bits_equal(a.cpu().numpy(), oracle.steps(u0, kappa, h, dt, 6))
