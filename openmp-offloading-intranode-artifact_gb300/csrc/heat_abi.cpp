@@ -77,9 +77,9 @@ int download(double *dst, const double *src, const heat_geom &g, cudaStream_t st
 void free_ctx(heat_ctx *c) {
   if (!c) return;
   void *ptrs[] = {c->u[0],   c->u[1],     c->rhs,      c->kappa,    c->ks[0],   c->ks[1],
-                  c->ks[2],  c->c0,       c->cf[0],    c->cf[1],    c->cf[2],   c->v[0],
-                  c->v[1],   c->carry[0], c->carry[1], c->fcf[0],   c->fcf[1],  c->fcf[2],
-                  c->frhs,   c->partials};
+                  c->ks[2],  c->c0,       c->cf[0],    c->cf[1],    c->cf[2],   c->kq,
+                  c->v[0],   c->v[1],     c->carry[0], c->carry[1], c->fcf[0],  c->fcf[1],
+                  c->fcf[2], c->frhs,     c->partials};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -94,9 +94,10 @@ int launch_step(heat_ctx *c) {
     e = heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, c->stream);
   else if (c->flags & HEAT_BITEXACT)
     e = heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, c->stream);
+  else if (c->kq)
+    e = heat::launch_fast_int(un, uo, c->rhs, c->kq, g, c->stream);
   else
-    e = heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, c->stream,
-                          (c->flags & HEAT_HWFP64) != 0);
+    e = heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, c->stream, true);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
   c->launches += 1;
   c->cur ^= 1;
@@ -205,9 +206,29 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
       c->launches += 1;
     }
   } else {
-    TRY(dalloc(&c->c0, g.elems));
-    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
-    {
+    bool use_int = !(c->flags & HEAT_HWFP64);
+    if (use_int) {
+      // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
+      // the FP64-pipe kernel when the fixed-point range check fails.
+      TRY(dalloc(&c->kq, g.elems));
+      int bad = 0;
+      int *d_bad = reinterpret_cast<int *>(c->partials);
+      cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+      if (e == cudaSuccess) e = heat::launch_kq_setup(c->kq, d_bad, kap, g, c->factor, c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "fixed-point setup"); goto fail; }
+      c->launches += 1;
+      if (bad) {
+        cudaFree(c->kq);
+        c->kq = nullptr;
+        use_int = false;
+      }
+    }
+    if (!use_int) {
+      TRY(dalloc(&c->c0, g.elems));
+      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
       cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);
       if (e != cudaSuccess) { rc = cuda_fail(e, "coefficients"); goto fail; }
       c->launches += 1;

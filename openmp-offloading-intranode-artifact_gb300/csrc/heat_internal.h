@@ -34,8 +34,9 @@ struct heat_ctx {
   // Per-form coefficient planes (only the ones the chosen kernel uses).
   double *kappa;            // raw conductivity (naive kernel)
   double *ks[3];            // face kappa sums kx, ky, kz (bit-exact kernel)
-  double *c0;               // centre weight 1 - sum of face weights (fast)
-  double *cf[3];            // face weights factor*(kappa_a+kappa_b) (fast)
+  double *c0;               // centre weight 1 - sum of face weights (fast, FP64 pipe)
+  double *cf[3];            // face weights factor*(kappa_a+kappa_b) (fast, FP64 pipe)
+  unsigned long long *kq;   // round(factor*kappa*2^64) (fast, integer pipes)
 
   // FP32C state.
   float *v[2];              // FP32 fields
@@ -75,6 +76,12 @@ cudaError_t launch_fast_coeffs(double *c0, double *const cf[3], const double *ka
 cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
                         const double *c0, double *const cf[3], const heat_geom &g,
                         cudaStream_t st, bool hw_only);
+
+// heat_fp64_int.cu
+cudaError_t launch_kq_setup(unsigned long long *K, int *bad, const double *kappa,
+                            const heat_geom &g, double factor, cudaStream_t st);
+cudaError_t launch_fast_int(double *u_new, const double *u_old, const double *rhs,
+                            const unsigned long long *K, const heat_geom &g, cudaStream_t st);
 
 // heat_reduce.cu
 cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,

@@ -19,6 +19,8 @@ pytestmark = pytest.mark.gpu
 
 FAST_MAX_REL = 1e-12
 FAST_REL_L2 = 1e-13
+# default FP64 form: integer-pipe kernel (flags 0) and FP64-pipe kernel (HEAT_HWFP64)
+FAST = (0, 4)
 
 
 @pytest.fixture(scope="module")
@@ -36,14 +38,14 @@ FORMS = {"bitexact": 1, "naive": 1 | 2}
 
 
 @pytest.mark.parametrize("path", golden_npz(), ids=lambda p: p.stem)
-@pytest.mark.parametrize("form", ["bitexact", "naive", "default"])
+@pytest.mark.parametrize("form", ["bitexact", "naive", "default", "default-hw"])
 def test_golden_reference_problem(H, path, form):
     z = np.load(path)
     n, steps, h, dt, T = z["meta"]
-    flags = FORMS.get(form, 0)
+    flags = FORMS.get(form, 4 if form == "default-hw" else 0)
     u, s, _ = solve(H, z["kappa"], z["u0"], h, dt, T=T, rhs=z["rhs"], flags=flags)
     assert s == int(steps)
-    if form == "default":
+    if form.startswith("default"):
         m = metrics(z["u"], u)
         assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
     else:
@@ -60,9 +62,10 @@ def test_reference_problem_larger(H, oracle, case):
     u_ex, s_ex, _ = solve(H, kappa, u0, h, dt, T=float(case["T"]), rhs=rhs, flags=1)
     assert s_ex == s_or
     assert bits_equal(u_ex, u_or)
-    u_fa, _, _ = solve(H, kappa, u0, h, dt, T=float(case["T"]), rhs=rhs, flags=0)
-    m = metrics(u_or, u_fa)
-    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    for fl in FAST:
+        u_fa, _, _ = solve(H, kappa, u0, h, dt, T=float(case["T"]), rhs=rhs, flags=fl)
+        m = metrics(u_or, u_fa)
+        assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, (fl, m)
 
 
 SHAPES = [(3, 3, 3), (4, 5, 6), (5, 4, 3), (33, 17, 9), (31, 33, 35), (64, 8, 40), (130, 67, 21)]
@@ -76,9 +79,10 @@ def test_odd_and_uneven_grids(H, oracle, shape):
     for flags in (1, 3):
         u, _, _ = solve(H, kappa, u0, h, dt, steps=23, flags=flags)
         assert bits_equal(u, u_or), flags
-    u, _, _ = solve(H, kappa, u0, h, dt, steps=23, flags=0)
-    m = metrics(u_or, u)
-    assert m["max_rel"] <= FAST_MAX_REL, m
+    for fl in FAST:
+        u, _, _ = solve(H, kappa, u0, h, dt, steps=23, flags=fl)
+        m = metrics(u_or, u)
+        assert m["max_rel"] <= FAST_MAX_REL, (fl, m)
 
 
 def test_config0_full(H, oracle):
@@ -89,9 +93,10 @@ def test_config0_full(H, oracle):
     assert bits_equal(u_ex, u_or)
     l2_or, cs_or = oracle.norm(u_or)
     assert l2 == pytest.approx(l2_or, rel=1e-13) and cs == pytest.approx(cs_or, rel=1e-13)
-    u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=100, flags=0)
-    m = metrics(u_or, u_fa)
-    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    for fl in FAST:
+        u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=100, flags=fl)
+        m = metrics(u_or, u_fa)
+        assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, (fl, m)
 
 
 def test_config1_reduced(H, oracle):
@@ -100,9 +105,10 @@ def test_config1_reduced(H, oracle):
     u_or = oracle.steps(u0, kappa, h, dt, 300)
     u_ex, _, _ = solve(H, kappa, u0, h, dt, steps=300, flags=1)
     assert bits_equal(u_ex, u_or)
-    u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=300, flags=0)
-    m = metrics(u_or, u_fa)
-    assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    for fl in FAST:
+        u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=300, flags=fl)
+        m = metrics(u_or, u_fa)
+        assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, (fl, m)
 
 
 def test_config1_full_size_short(H, oracle):
@@ -142,7 +148,7 @@ def test_nonzero_boundary_is_never_written(H):
     b = np.ones(u0.shape, dtype=bool)
     b[1:-1, 1:-1, 1:-1] = False
     u0[b] = rng.uniform(1, 2, b.sum())
-    for flags in (0, 1, 3):
+    for flags in (0, 1, 3, 4):
         u, _, _ = solve(H, kappa, u0, h, dt, steps=17, flags=flags)
         assert bits_equal(u[b], u0[b]), flags
 
