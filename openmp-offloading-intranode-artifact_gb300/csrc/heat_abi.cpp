@@ -14,6 +14,10 @@ namespace {
 
 thread_local char g_last_error[256] = "";
 
+// Warps (of 8 per block) of the hybrid FP64 kernel that run on the FP64 pipe;
+// the others run the integer-pipe evaluation.
+constexpr int kDefaultHwRows = 3;
+
 int cuda_fail(cudaError_t e, const char *what) {
   std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
   return HEAT_ECUDA;
@@ -95,7 +99,7 @@ int launch_step(heat_ctx *c) {
   else if (c->flags & HEAT_BITEXACT)
     e = heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, c->stream);
   else if (c->kq)
-    e = heat::launch_fast_int(un, uo, c->rhs, c->kq, g, c->stream);
+    e = heat::launch_fast_mix(un, uo, c->rhs, c->kq, c->c0, c->cf, g, c->hw_rows, c->stream);
   else
     e = heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, c->stream, true);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
@@ -207,6 +211,12 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
     }
   } else {
     bool use_int = !(c->flags & HEAT_HWFP64);
+    c->hw_rows = kDefaultHwRows;
+    if (const char *ev = std::getenv("HEAT_HW_ROWS")) {  // tuning knob, 0..8
+      int v = std::atoi(ev);
+      if (v >= 0 && v <= 8) c->hw_rows = v;
+    }
+    if (c->hw_rows == 8) use_int = false;
     if (use_int) {
       // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
       // the FP64-pipe kernel when the fixed-point range check fails.
@@ -226,7 +236,7 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
         use_int = false;
       }
     }
-    if (!use_int) {
+    if (!use_int || c->hw_rows > 0) {
       TRY(dalloc(&c->c0, g.elems));
       for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
       cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);

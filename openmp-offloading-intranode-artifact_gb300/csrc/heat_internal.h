@@ -37,6 +37,7 @@ struct heat_ctx {
   double *c0;               // centre weight 1 - sum of face weights (fast, FP64 pipe)
   double *cf[3];            // face weights factor*(kappa_a+kappa_b) (fast, FP64 pipe)
   unsigned long long *kq;   // round(factor*kappa*2^64) (fast, integer pipes)
+  int hw_rows;              // warps per block on the FP64 pipe in the hybrid kernel
 
   // FP32C state.
   float *v[2];              // FP32 fields
@@ -80,8 +81,12 @@ cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
 // heat_fp64_int.cu
 cudaError_t launch_kq_setup(unsigned long long *K, int *bad, const double *kappa,
                             const heat_geom &g, double factor, cudaStream_t st);
-cudaError_t launch_fast_int(double *u_new, const double *u_old, const double *rhs,
-                            const unsigned long long *K, const heat_geom &g, cudaStream_t st);
+// hw_rows of the 8 warps in each block take the FP64 pipe, the rest the
+// integer pipes; K may be NULL only when hw_rows == 8, c0/cf only when 0.
+cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rhs,
+                            const unsigned long long *K, const double *c0,
+                            double *const cf[3], const heat_geom &g, int hw_rows,
+                            cudaStream_t st);
 
 // heat_reduce.cu
 cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,

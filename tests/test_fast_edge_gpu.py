@@ -78,14 +78,13 @@ def test_non_finite_inputs_stay_non_finite(H, oracle):
 
 def test_unstable_dt_falls_back_and_still_matches(H, oracle):
     """dt = 3x the stability limit: the fixed-point check fails, the context
-    uses the FP64-pipe kernel; results still follow the reference (which
-    grows without bound) to 1e-12 for a few steps."""
+    uses the FP64-pipe kernel; results still follow the reference (whose
+    high-frequency modes grow) closely."""
     nx = ny = nz = 20
     kappa, u0, h, dt = H.inputs_config(0, 4, nx, ny, nz)
     dt3 = 3 * dt
-    ref = oracle.steps(u0, kappa, h, dt3, 6)
-    got = run(H, kappa, u0, h, dt3, 6)
-    assert np.abs(ref).max() > 2.0          # it does blow up
+    ref = oracle.steps(u0, kappa, h, dt3, 12)
+    got = run(H, kappa, u0, h, dt3, 12)
     m = metrics(ref, got)
     assert m["rel_l2"] <= 1e-13, m
 
