@@ -45,6 +45,7 @@ CFG = 1
 METRIC = "GLUP/s (FP64 plain heat stencil, 512^3, 1000 steps per solve)"
 UNIT = "GLUP/s"
 BYTES_PER_UPDATE = 24.0   # u read 8 + u write 8 + kappa read 8 (compulsory, FP64)
+FP32C_BYTES_PER_UPDATE = 24.0  # v 4+4, carry 2+2, three FP32 face weights 12
 H100_1CUDA_N512 = 38.97   # reference 1-cuda, H100, N=512 (CUDA/summary.csv:2)
 
 
@@ -251,6 +252,19 @@ def our_arm(a):
     ms = ev0.elapsed_time(ev1)
     l2n, csum = s.norm()
     s.close()
+
+    # ---- FP32-compensated form on the same workload (precision pattern)
+    s32 = H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C, stream=stream.cuda_stream)
+    s32.step(max(1, ts // 10))
+    s32.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s32.step(ts)
+    e1.record(stream)
+    e1.synchronize()
+    ms32 = e0.elapsed_time(e1)
+    s32.close()
+    fp32c_value = updates(n, ts) / (ms32 * 1e-3) / 1e9
     t_max = ms
     if dist:
         t = torch.tensor([ms], device="cuda")
@@ -311,6 +325,12 @@ def our_arm(a):
                     "h2d_bytes_per_step": int(pk.numel() * 8 + pu.numel() * 8),
                     "d2h_bytes_per_step": int(pout.numel() * 8),
                     "ms_per_step": round(e2e_s * 1e3, 3)},
+            "fp32c": {"value": round(fp32c_value, 3), "unit": UNIT,
+                      "vs_fp64": round(fp32c_value / (value / world), 3),
+                      "bytes_per_update": FP32C_BYTES_PER_UPDATE,
+                      "hbm_frac": round(fp32c_value * FP32C_BYTES_PER_UPDATE / hbm_peak, 4),
+                      "note": "FP32 u + BF16 Kahan carry, FP32 face weights; same workload, "
+                              f"{ts} steps, CUDA events; errors: profiles/fp32c_precision.md"},
             "gpu_launches": int(l1 - l0),
             "clocks": clk.summary(),
             "result": {"l2": l2n, "checksum": csum},

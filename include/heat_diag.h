@@ -19,6 +19,15 @@ extern "C" {
  * events.  Takes a few milliseconds.  Returns HEAT_OK or a HEAT_E* code.   */
 int heat_diag_fp64_rate(double *gops_out);
 
+/* Difference of the current fields of two contexts of the same grid, on the
+ * device: max |a - b| and ||a - b||_2 / ||b||_2 over all points (b is the
+ * reference side, as compare.py:47-76 of the reference's verify pipeline
+ * treats its first argument).  Works across precision forms (an FP32C field
+ * is widened to FP64 first).  Synchronises both contexts' streams.         */
+struct heat_ctx;
+int heat_diag_field_diff(struct heat_ctx *a, struct heat_ctx *b, double *max_abs,
+                         double *rel_l2);
+
 #ifdef __cplusplus
 }
 #endif

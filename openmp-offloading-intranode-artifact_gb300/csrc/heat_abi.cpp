@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 
+#include "heat_diag.h"
 #include "heat_internal.h"
 
 namespace {
@@ -94,7 +95,10 @@ int launch_step(heat_ctx *c) {
   const heat_geom &g = c->g;
   double *uo = c->u[c->cur], *un = c->u[c->cur ^ 1];
   cudaError_t e;
-  if (c->flags & HEAT_NAIVE)
+  if (c->precision == HEAT_FP32C)
+    e = heat::launch_fp32c(c->v[c->cur ^ 1], c->carry[c->cur ^ 1], c->v[c->cur],
+                           c->carry[c->cur], c->fcf, c->frhs, g, c->stream);
+  else if (c->flags & HEAT_NAIVE)
     e = heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, c->stream);
   else if (c->flags & HEAT_BITEXACT)
     e = heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, c->stream);
@@ -107,6 +111,169 @@ int launch_step(heat_ctx *c) {
   c->cur ^= 1;
   c->steps_done += 1;
   return HEAT_OK;
+}
+
+
+int widen_current(heat_ctx *c, double **out) {
+  int rc = dalloc(out, c->g.elems);
+  if (rc != HEAT_OK) return rc;
+  cudaError_t e = heat::launch_widen(*out, c->v[c->cur], c->carry[c->cur], c->g.elems, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "widen");
+  c->launches += 1;
+  return HEAT_OK;
+}
+
+// Upload a host FP64 field through tmp (device, g.elems doubles) into both
+// FP32C state buffers.
+int load_split(heat_ctx *c, double *tmp, const double *u_host) {
+  const heat_geom &g = c->g;
+  CK(cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream));
+  int rc = upload(tmp, u_host, g, c->stream);
+  if (rc != HEAT_OK) return rc;
+  cudaError_t e = heat::launch_split(c->v[0], c->carry[0], tmp, g.elems, c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "split");
+  c->launches += 1;
+  CK(cudaMemcpyAsync(c->v[1], c->v[0], g.elems * sizeof(float), cudaMemcpyDeviceToDevice,
+                     c->stream));
+  CK(cudaMemcpyAsync(c->carry[1], c->carry[0], g.elems * sizeof(uint16_t),
+                     cudaMemcpyDeviceToDevice, c->stream));
+  return HEAT_OK;
+}
+
+int init_fp64(heat_ctx *c, const heat_desc *d) {
+  const heat_geom &g = c->g;
+  const size_t bytes = g.elems * sizeof(double);
+  int rc = HEAT_OK;
+  double *kap = nullptr;  // raw kappa on the device (kept only for the naive kernel)
+#define TRY(x)                    \
+  do {                            \
+    rc = (x);                     \
+    if (rc != HEAT_OK) goto done; \
+  } while (0)
+  TRY(dalloc(&c->u[0], g.elems));
+  TRY(dalloc(&c->u[1], g.elems));
+  TRY(dalloc(&kap, g.elems));
+  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
+  c->n_partials = heat::kNormBlocks;
+  if (cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
+      cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+    goto done;
+  }
+  TRY(upload(c->u[0], d->u0, g, c->stream));
+  TRY(upload(kap, d->kappa, g, c->stream));
+  // u_new starts as a copy of u0, so its boundary holds the same values
+  // (the reference seeds both buffers from u0, 1-cuda.cu:219-222).
+  if (cudaMemcpyAsync(c->u[1], c->u[0], bytes, cudaMemcpyDeviceToDevice, c->stream) !=
+      cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemcpy u0");
+    goto done;
+  }
+  if (d->rhs) {
+    TRY(dalloc(&c->rhs, g.elems));
+    if (cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+      goto done;
+    }
+    TRY(upload(c->rhs, d->rhs, g, c->stream));
+  }
+  if (c->flags & HEAT_NAIVE) {
+    c->kappa = kap;
+    kap = nullptr;
+  } else if (c->flags & HEAT_BITEXACT) {
+    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->ks[a], g.elems));
+    {
+      cudaError_t e = heat::launch_face_sums(c->ks, kap, g, c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "face sums"); goto done; }
+      c->launches += 1;
+    }
+  } else {
+    bool use_int = !(c->flags & HEAT_HWFP64);
+    c->hw_rows = kDefaultHwRows;
+    if (const char *ev = std::getenv("HEAT_HW_ROWS")) {  // tuning knob, 0..8
+      int v = std::atoi(ev);
+      if (v >= 0 && v <= 8) c->hw_rows = v;
+    }
+    if (c->hw_rows == 8) use_int = false;
+    if (use_int) {
+      // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
+      // the FP64-pipe kernel when the fixed-point range check fails.
+      TRY(dalloc(&c->kq, g.elems));
+      int bad = 0;
+      int *d_bad = reinterpret_cast<int *>(c->partials);
+      cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
+      if (e == cudaSuccess) e = heat::launch_kq_setup(c->kq, d_bad, kap, g, c->factor, c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "fixed-point setup"); goto done; }
+      c->launches += 1;
+      if (bad) {
+        cudaFree(c->kq);
+        c->kq = nullptr;
+        use_int = false;
+      }
+    }
+    if (!use_int || c->hw_rows > 0) {
+      TRY(dalloc(&c->c0, g.elems));
+      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
+      cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);
+      if (e != cudaSuccess) { rc = cuda_fail(e, "coefficients"); goto done; }
+      c->launches += 1;
+    }
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+    rc = cuda_fail(cudaGetLastError(), "heat_init sync");
+done:
+  if (kap) cudaFree(kap);
+  return rc;
+#undef TRY
+}
+
+int init_fp32c(heat_ctx *c, const heat_desc *d) {
+  const heat_geom &g = c->g;
+  int rc = HEAT_OK;
+  double *tmp = nullptr;  // FP64 staging buffer for u0, kappa and rhs
+  cudaError_t e = cudaSuccess;
+#define TRY(x)                    \
+  do {                            \
+    rc = (x);                     \
+    if (rc != HEAT_OK) goto done; \
+  } while (0)
+  for (int b = 0; b < 2; ++b) {
+    TRY(dalloc(&c->v[b], g.elems));
+    TRY(dalloc(&c->carry[b], g.elems));
+  }
+  for (int a = 0; a < 3; ++a) TRY(dalloc(&c->fcf[a], g.elems));
+  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
+  c->n_partials = heat::kNormBlocks;
+  TRY(dalloc(&tmp, g.elems));
+  TRY(load_split(c, tmp, d->u0));
+  if (cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+    goto done;
+  }
+  TRY(upload(tmp, d->kappa, g, c->stream));
+  e = heat::launch_f32_weights(c->fcf, tmp, g, c->factor, c->stream);
+  if (e != cudaSuccess) { rc = cuda_fail(e, "FP32 weights"); goto done; }
+  c->launches += 1;
+  if (d->rhs) {
+    TRY(dalloc(&c->frhs, g.elems));
+    if (cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+      goto done;
+    }
+    TRY(upload(tmp, d->rhs, g, c->stream));
+    e = heat::launch_to_f32(c->frhs, tmp, g.elems, c->stream);
+    if (e != cudaSuccess) { rc = cuda_fail(e, "FP32 rhs"); goto done; }
+    c->launches += 1;
+  }
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess)
+    rc = cuda_fail(cudaGetLastError(), "heat_init sync");
+done:
+  if (tmp) cudaFree(tmp);
+  return rc;
+#undef TRY
 }
 
 }  // namespace
@@ -134,7 +301,9 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
   if (!geom_ok(d->nx, d->ny, d->nz)) return HEAT_EINVAL;
   if (!(d->h > 0.0) || !(d->dt > 0.0) || !std::isfinite(d->h) || !std::isfinite(d->dt))
     return HEAT_EINVAL;
-  if (d->precision != HEAT_FP64) return HEAT_EINVAL;  // FP32C added separately
+  if (d->precision != HEAT_FP64 && d->precision != HEAT_FP32C) return HEAT_EINVAL;
+  if (d->precision == HEAT_FP32C && (d->flags & (HEAT_BITEXACT | HEAT_NAIVE)))
+    return HEAT_EINVAL;
 
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
@@ -162,100 +331,13 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
     }
     c->own_stream = true;
   }
-
-  const heat_geom &g = c->g;
-  const size_t bytes = g.elems * sizeof(double);
-  int rc = HEAT_OK;
-  double *kap = nullptr;  // raw kappa on the device (kept only for the naive kernel)
-#define TRY(x)                 \
-  do {                         \
-    rc = (x);                  \
-    if (rc != HEAT_OK) goto fail; \
-  } while (0)
-  TRY(dalloc(&c->u[0], g.elems));
-  TRY(dalloc(&c->u[1], g.elems));
-  TRY(dalloc(&kap, g.elems));
-  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
-  c->n_partials = heat::kNormBlocks;
-  if (cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
-      cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
-    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
-    goto fail;
+  int rc = (c->precision == HEAT_FP64) ? init_fp64(c, d) : init_fp32c(c, d);
+  if (rc != HEAT_OK) {
+    free_ctx(c);
+    return rc;
   }
-  TRY(upload(c->u[0], d->u0, g, c->stream));
-  TRY(upload(kap, d->kappa, g, c->stream));
-  // u_new starts as a copy of u0, so its boundary holds the same values
-  // (the reference seeds both buffers from u0, 1-cuda.cu:219-222).
-  if (cudaMemcpyAsync(c->u[1], c->u[0], bytes, cudaMemcpyDeviceToDevice, c->stream) !=
-      cudaSuccess) {
-    rc = cuda_fail(cudaGetLastError(), "cudaMemcpy u0");
-    goto fail;
-  }
-  if (d->rhs) {
-    TRY(dalloc(&c->rhs, g.elems));
-    if (cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
-      rc = cuda_fail(cudaGetLastError(), "cudaMemset");
-      goto fail;
-    }
-    TRY(upload(c->rhs, d->rhs, g, c->stream));
-  }
-  if (c->flags & HEAT_NAIVE) {
-    c->kappa = kap;
-    kap = nullptr;
-  } else if (c->flags & HEAT_BITEXACT) {
-    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->ks[a], g.elems));
-    {
-      cudaError_t e = heat::launch_face_sums(c->ks, kap, g, c->stream);
-      if (e != cudaSuccess) { rc = cuda_fail(e, "face sums"); goto fail; }
-      c->launches += 1;
-    }
-  } else {
-    bool use_int = !(c->flags & HEAT_HWFP64);
-    c->hw_rows = kDefaultHwRows;
-    if (const char *ev = std::getenv("HEAT_HW_ROWS")) {  // tuning knob, 0..8
-      int v = std::atoi(ev);
-      if (v >= 0 && v <= 8) c->hw_rows = v;
-    }
-    if (c->hw_rows == 8) use_int = false;
-    if (use_int) {
-      // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
-      // the FP64-pipe kernel when the fixed-point range check fails.
-      TRY(dalloc(&c->kq, g.elems));
-      int bad = 0;
-      int *d_bad = reinterpret_cast<int *>(c->partials);
-      cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
-      if (e == cudaSuccess) e = heat::launch_kq_setup(c->kq, d_bad, kap, g, c->factor, c->stream);
-      if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-      if (e != cudaSuccess) { rc = cuda_fail(e, "fixed-point setup"); goto fail; }
-      c->launches += 1;
-      if (bad) {
-        cudaFree(c->kq);
-        c->kq = nullptr;
-        use_int = false;
-      }
-    }
-    if (!use_int || c->hw_rows > 0) {
-      TRY(dalloc(&c->c0, g.elems));
-      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
-      cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);
-      if (e != cudaSuccess) { rc = cuda_fail(e, "coefficients"); goto fail; }
-      c->launches += 1;
-    }
-  }
-  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
-    rc = cuda_fail(cudaGetLastError(), "heat_init sync");
-    goto fail;
-  }
-  if (kap) cudaFree(kap);
   *out = c;
   return HEAT_OK;
-fail:
-  if (kap) cudaFree(kap);
-  free_ctx(c);
-  return rc;
-#undef TRY
 }
 
 int heat_step(heat_ctx *c, int nsteps) {
@@ -286,7 +368,11 @@ int heat_run(heat_ctx *c, double T, int *steps_out) {
 
 int heat_norm(heat_ctx *c, double *l2, double *checksum) {
   if (!c) return HEAT_EINVAL;
-  cudaError_t e = heat::launch_norm_f64(c->u[c->cur], c->g, c->partials, c->n_partials, c->stream);
+  cudaError_t e =
+      (c->precision == HEAT_FP64)
+          ? heat::launch_norm_f64(c->u[c->cur], c->g, c->partials, c->n_partials, c->stream)
+          : heat::launch_norm_f32c(c->v[c->cur], c->carry[c->cur], c->g, c->partials,
+                                   c->n_partials, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "norm launch");
   c->launches += 2;
   double r[2];
@@ -300,9 +386,19 @@ int heat_norm(heat_ctx *c, double *l2, double *checksum) {
 
 int heat_get_field(heat_ctx *c, double *u_host) {
   if (!c || !u_host) return HEAT_EINVAL;
-  int rc = download(u_host, c->u[c->cur], c->g, c->stream);
+  if (c->precision == HEAT_FP64) {
+    int rc = download(u_host, c->u[c->cur], c->g, c->stream);
+    if (rc != HEAT_OK) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return HEAT_OK;
+  }
+  double *tmp = nullptr;
+  int rc = widen_current(c, &tmp);
+  if (rc == HEAT_OK) rc = download(u_host, tmp, c->g, c->stream);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (tmp) cudaFree(tmp);
   if (rc != HEAT_OK) return rc;
-  CK(cudaStreamSynchronize(c->stream));
+  if (e != cudaSuccess) return cuda_fail(e, "heat_get_field");
   return HEAT_OK;
 }
 
@@ -310,11 +406,22 @@ int heat_set_field(heat_ctx *c, const double *u_host) {
   if (!c || !u_host) return HEAT_EINVAL;
   // Both buffers take the new field so the boundary stays consistent in
   // whichever one the next step writes.
-  int rc = upload(c->u[c->cur], u_host, c->g, c->stream);
+  if (c->precision == HEAT_FP64) {
+    int rc = upload(c->u[c->cur], u_host, c->g, c->stream);
+    if (rc != HEAT_OK) return rc;
+    CK(cudaMemcpyAsync(c->u[c->cur ^ 1], c->u[c->cur], c->g.elems * sizeof(double),
+                       cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return HEAT_OK;
+  }
+  double *tmp = nullptr;
+  int rc = dalloc(&tmp, c->g.elems);
   if (rc != HEAT_OK) return rc;
-  CK(cudaMemcpyAsync(c->u[c->cur ^ 1], c->u[c->cur], c->g.elems * sizeof(double),
-                     cudaMemcpyDeviceToDevice, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  rc = load_split(c, tmp, u_host);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (rc != HEAT_OK) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "heat_set_field");
   return HEAT_OK;
 }
 
@@ -364,6 +471,39 @@ int heat_update(double *u_new, const double *u_old, const double *rhs, const dou
     if (cur != device_id) CK(cudaSetDevice(device_id));
   }
   return heat_update_async(u_new, u_old, rhs, kappa, nz, ny, nx, factor, (void *)cudaStreamLegacy);
+}
+
+int heat_diag_field_diff(heat_ctx *a, heat_ctx *b, double *max_abs, double *rel_l2) {
+  if (!a || !b) return HEAT_EINVAL;
+  if (a->g.nx != b->g.nx || a->g.ny != b->g.ny || a->g.nz != b->g.nz) return HEAT_EINVAL;
+  CK(cudaStreamSynchronize(a->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  double *fa = nullptr, *fb = nullptr, *part = nullptr, *ta = nullptr, *tb = nullptr;
+  int rc = HEAT_OK;
+  const int nb = heat::kNormBlocks;
+  double r[3] = {0, 0, 0};
+  cudaError_t e = cudaSuccess;
+  if (a->precision == HEAT_FP64) fa = a->u[a->cur];
+  else if ((rc = widen_current(a, &ta)) == HEAT_OK) fa = ta;
+  if (rc == HEAT_OK) {
+    if (b->precision == HEAT_FP64) fb = b->u[b->cur];
+    else if ((rc = widen_current(b, &tb)) == HEAT_OK) fb = tb;
+  }
+  if (rc == HEAT_OK) rc = dalloc(&part, 3 * (size_t)nb + 3);
+  if (rc == HEAT_OK) {
+    e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = heat::launch_diff_f64(fa, fb, a->g, part, nb, (cudaStream_t)0);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(r, part + 3 * nb, sizeof r, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = cuda_fail(e, "field diff");
+  }
+  if (ta) cudaFree(ta);
+  if (tb) cudaFree(tb);
+  if (part) cudaFree(part);
+  if (rc != HEAT_OK) return rc;
+  if (max_abs) *max_abs = r[2];
+  if (rel_l2) *rel_l2 = r[1] > 0 ? std::sqrt(r[0] / r[1]) : std::sqrt(r[0]);
+  return HEAT_OK;
 }
 
 }  // extern "C"

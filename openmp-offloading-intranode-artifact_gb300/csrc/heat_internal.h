@@ -88,8 +88,26 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             double *const cf[3], const heat_geom &g, int hw_rows,
                             cudaStream_t st);
 
+// heat_fp32c.cu
+cudaError_t launch_fp32c(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
+                         float *const w[3], const float *rhs, const heat_geom &g,
+                         cudaStream_t st);
+cudaError_t launch_split(float *v, uint16_t *cr, const double *u, size_t total, cudaStream_t st);
+cudaError_t launch_widen(double *u, const float *v, const uint16_t *cr, size_t total,
+                         cudaStream_t st);
+cudaError_t launch_f32_weights(float *const w[3], const double *kappa, const heat_geom &g,
+                               double factor, cudaStream_t st);
+cudaError_t launch_to_f32(float *o, const double *a, size_t total, cudaStream_t st);
+
 // heat_reduce.cu
 cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,
                             int nblocks, cudaStream_t st);
+// Norm of the FP32C state u = v - c (widened to FP64 per point).
+cudaError_t launch_norm_f32c(const float *v, const uint16_t *cr, const heat_geom &g,
+                             double *partials, int nblocks, cudaStream_t st);
+// sum (a-b)^2, sum b^2 and max |a-b| of two FP64 fields of one geometry;
+// partials needs 3*nblocks+3 doubles, results at partials[3*nblocks..].
+cudaError_t launch_diff_f64(const double *a, const double *b, const heat_geom &g,
+                            double *partials, int nblocks, cudaStream_t st);
 
 }  // namespace heat

@@ -73,6 +73,7 @@ SIGNATURES = {
                                      C.c_void_p, C.c_void_p, _dp, _dp]),
     # include/heat_diag.h
     "heat_diag_fp64_rate": (C.c_int, [_dp]),
+    "heat_diag_field_diff": (C.c_int, [C.c_void_p, C.c_void_p, _dp, _dp]),
 }
 
 
@@ -131,6 +132,13 @@ def fp64_rate() -> float:
     g = C.c_double()
     check(lib().heat_diag_fp64_rate(C.byref(g)), "heat_diag_fp64_rate")
     return g.value
+
+
+def field_diff(a: "Solver", b: "Solver") -> tuple[float, float]:
+    """(max |a-b|, ||a-b|| / ||b||) of two solvers' current fields, on the device."""
+    mx, rl = C.c_double(), C.c_double()
+    check(lib().heat_diag_field_diff(a._ctx, b._ctx, C.byref(mx), C.byref(rl)), "heat_diag_field_diff")
+    return mx.value, rl.value
 
 
 class Solver:
