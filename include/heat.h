@@ -100,6 +100,24 @@ int heat_run(heat_ctx *c, double T, int *steps_out);
  * verify pipeline.  Synchronises the context's stream.                      */
 int heat_norm(heat_ctx *c, double *l2, double *checksum);
 
+/* L2 norm and checksum of a caller-owned FP64 device field u (dense k-j-i,
+ * row length nx, nz*ny*nx doubles) that allocates nothing: no cudaMalloc,
+ * no cudaFree, no host allocation.  No counterpart in the reference.
+ * For callers that must not allocate while they run -- a serving loop whose
+ * HBM is all committed to its admission budget or to another allocator, or a
+ * monitoring hook between time steps that cannot take the device-wide stall
+ * of cudaFree/cudaMalloc.  Its scratch is a static device array sized for
+ * nz <= HEAT_NORM_NOALLOC_MAX_NZ planes (256 KiB, held by every GPU that loads
+ * the library); larger nz returns HEAT_EINVAL.  The first call on a device
+ * looks the array's address up (do it before any stream capture).  All calls
+ * on a device share the array: calls that overlap on the GPU race, so issue
+ * them from one stream.  Runs on stream (cudaStream_t, NULL = legacy default)
+ * and synchronises it.  Summation order differs from heat_norm's, so results
+ * agree with it to rounding (<= 1e-13 relative), not bit for bit.          */
+#define HEAT_NORM_NOALLOC_MAX_NZ 16384
+int heat_norm_noalloc(const double *u, int nz, int ny, int nx, double *l2,
+                      double *checksum, void *stream);
+
 /* Copy the current field (the reference's u_old after the swap,
  * 1-cuda.cu:264) to / from a host array of nz*ny*nx doubles, k-j-i.
  * For HEAT_FP32C the FP32 value plus its carry is widened to FP64.          */

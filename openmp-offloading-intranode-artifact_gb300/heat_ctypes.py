@@ -68,6 +68,7 @@ SIGNATURES = {
                               C.c_int, C.c_int, C.c_int, C.c_double, C.c_int]),
     "heat_update_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
+    "heat_norm_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_void_p]),
     "heat_inputs_reference": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _dp, _dp]),
     "heat_inputs_config": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int,
                                      C.c_void_p, C.c_void_p, _dp, _dp]),
