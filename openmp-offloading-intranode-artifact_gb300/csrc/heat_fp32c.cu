@@ -15,22 +15,16 @@
 // round-to-nearest intrinsics so no contraction or reassociation can remove
 // them.  Bytes per update: v 4+4, carry 2+2, face weights 3x4.
 
-#include <cuda_bf16.h>
-
 #include "heat_internal.h"
+#include "heat_walk.cuh"
 
 namespace heat {
 namespace {
 
 constexpr int TX = 32, TY = 8;
 
-__device__ __forceinline__ float bf2f(uint16_t b) {
-  return __uint_as_float(((unsigned)b) << 16);
-}
-__device__ __forceinline__ uint16_t f2bf(float x) {
-  __nv_bfloat16 h = __float2bfloat16_rn(x);
-  return *reinterpret_cast<uint16_t *>(&h);
-}
+using walk::bf2f;
+using walk::f2bf;
 
 template <bool RHS>
 __global__ void __launch_bounds__(TX *TY)
@@ -44,27 +38,8 @@ __global__ void __launch_bounds__(TX *TY)
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
   if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
-  size_t c = (size_t)kb * S + (size_t)j * P + i;
-  float vd = v[c - S], vc = v[c];
-  float wd = wz[c - S];
-  for (int k = kb; k < ke; ++k, c += S) {
-    const float vu = v[c + S], wu = wz[c];
-    float d = RHS ? rhs[c] : 0.0f;
-    d = fmaf(wx[c], v[c + 1] - vc, d);
-    d = fmaf(wx[c - 1], v[c - 1] - vc, d);
-    d = fmaf(wy[c], v[c + P] - vc, d);
-    d = fmaf(wy[c - P], v[c - P] - vc, d);
-    d = fmaf(wu, vu - vc, d);
-    d = fmaf(wd, vd - vc, d);
-    const float y = __fsub_rn(d, bf2f(cr[c]));
-    const float t = __fadd_rn(vc, y);
-    const float cc = __fsub_rn(__fsub_rn(t, vc), y);
-    vn[c] = t;
-    cn[c] = f2bf(cc);
-    vd = vc;
-    vc = vu;
-    wd = wu;
-  }
+  const size_t c = (size_t)kb * S + (size_t)j * P + i;
+  walk::walk_fp32c<RHS>(vn, cn, v, cr, wx, wy, wz, rhs, P, S, c, kb, ke);
 }
 
 // Split an FP64 field into (v, c) with v = fl32(u), c = bf16(v - u); padding 0.

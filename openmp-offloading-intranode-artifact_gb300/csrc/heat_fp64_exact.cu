@@ -16,21 +16,13 @@
 // plane k as F of plane k+1 and stays bit-identical.
 
 #include "heat_internal.h"
+#include "heat_walk.cuh"
 
 namespace heat {
 namespace {
 
-__device__ __forceinline__ double flux(double ksum, double ub, double ua) {
-  return __dmul_rn(ksum, __dsub_rn(ub, ua));
-}
-
-// base is u + rhs (or u alone when the problem has no source term: u + 0.0
-// equals u for every value but -0.0, which these fields never hold).
-__device__ __forceinline__ double combine(double base, double factor, double A, double B,
-                                          double C, double D, double E, double F) {
-  double s = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(A, B), C), D), E), F);
-  return __dadd_rn(base, __dmul_rn(factor, s));
-}
+using walk::combine;
+using walk::flux;
 
 // One thread per point, the reference CUDA kernel's shape (block 8x8x8,
 // 1-cuda.cu:85-131), arbitrary row pitch.
@@ -100,20 +92,8 @@ __global__ void __launch_bounds__(TX *TY)
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
   if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
-  size_t c = (size_t)kb * S + (size_t)j * P + i;
-  double uc = u[c];
-  double F = flux(kz[c - S], uc, u[c - S]);
-  for (int k = kb; k < ke; ++k, c += S) {
-    double uu = u[c + S];
-    double A = flux(kx[c], u[c + 1], uc);
-    double B = flux(kx[c - 1], uc, u[c - 1]);
-    double C = flux(ky[c], u[c + P], uc);
-    double D = flux(ky[c - P], uc, u[c - P]);
-    double E = flux(kz[c], uu, uc);
-    un[c] = combine(RHS ? __dadd_rn(uc, rhs[c]) : uc, factor, A, B, C, D, E, F);
-    F = E;
-    uc = uu;
-  }
+  const size_t c = (size_t)kb * S + (size_t)j * P + i;
+  walk::walk_exact_faces<RHS>(un, u, rhs, kx, ky, kz, P, S, c, kb, ke, factor);
 }
 
 __global__ void k_face_sums(double *__restrict__ kx, double *__restrict__ ky,

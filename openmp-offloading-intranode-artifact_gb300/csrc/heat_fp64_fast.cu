@@ -11,6 +11,7 @@
 // 26 as written (17 with shared face fluxes).
 
 #include "heat_internal.h"
+#include "heat_walk.cuh"
 
 namespace heat {
 namespace {
@@ -55,23 +56,8 @@ __global__ void __launch_bounds__(TX *TY)
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
   if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
-  size_t c = (size_t)kb * S + (size_t)j * P + i;
-  double ud = u[c - S], uc = u[c];
-  double wd = cz[c - S];
-  for (int k = kb; k < ke; ++k, c += S) {
-    double uu = u[c + S], wu = cz[c];
-    double acc = RHS ? fma(c0[c], uc, rhs[c]) : c0[c] * uc;
-    acc = fma(cx[c], u[c + 1], acc);
-    acc = fma(cx[c - 1], u[c - 1], acc);
-    acc = fma(cy[c], u[c + P], acc);
-    acc = fma(cy[c - P], u[c - P], acc);
-    acc = fma(wu, uu, acc);
-    acc = fma(wd, ud, acc);
-    un[c] = acc;
-    ud = uc;
-    uc = uu;
-    wd = wu;
-  }
+  const size_t c = (size_t)kb * S + (size_t)j * P + i;
+  walk::walk_hw<RHS>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
 }
 
 int choose_kchunk(const heat_geom &g) {

@@ -1,0 +1,289 @@
+// Per-column "walks" shared by the single-grid kernels and the batched
+// persistent kernel: each walks one (i, j) column of a grid over planes
+// [kb, ke), z-neighbours held in registers, and writes the new values.  The
+// same code runs alone and in a batch, so a grid's results do not depend on
+// how it was launched.
+//
+// Integer-pipe evaluation of the default FP64 form (walk_int):
+// GB300's FP64 pipe retires about 2 lane-operations per clock per SM, while
+// its integer pipes retire 64 (logic, shifts, IMAD) to 128 (IADD) lane-ops
+// per clock and run concurrently with it.  walk_int evaluates the update
+//
+//   u_new = uC + rhs + sum_f w_f (u_f - uC),   w_f = factor (kappa_a + kappa_b)
+//
+// (the reference's expression, OpenMP_Single_Source/heat3D_variable_coeff.c:
+// 174-181, regrouped) in 64-bit fixed point and rounds once to FP64:
+//
+//   1. each FP64 value x = m 2^(e-1075) (m signed, |m| < 2^53; subnormals
+//      decoded exactly) is aligned to the largest exponent E of the cell's
+//      stencil:  A = (m << 9) >> (E - e),  so |A| < 2^62 and the unit of A is
+//      2^(E-1084);
+//   2. differences D_f = A_f - A_C are exact;
+//   3. face weights are exact integer sums W_f = K_a + K_b of the per-point
+//      K = round(factor kappa 2^64), computed once per context from an
+//      error-free product, so sum_f w_f and the centre weight 1 - sum_f w_f
+//      are represented exactly;
+//   4. acc = A_C + A_rhs + sum_f D_f W_f / 2^64, each product's high word
+//      formed from the three 32x32 partial products that reach it;
+//   5. acc is rounded to nearest-even FP64.
+// The truncations in steps 1 and 4 are below 2^-57 of the largest term, so
+// the result is within 0.5 ulp (+ ~2^-56 relative) of the exact value of the
+// update with these weights: as accurate as the reference's own FP64
+// evaluation, and held to <= 1e-12 relative error against it.
+//
+// The representation needs |acc| < 2^63, which holds when every centre weight
+// 1 - sum_f w_f is >= 0 (the explicit scheme's stability condition) and each
+// factor*kappa < 1/4.  k_kq_setup checks both; contexts that fail it use the
+// FP64-pipe kernel alone.  Infinite or NaN inputs in a stencil take a
+// per-point FP64 path.
+
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace heat {
+namespace walk {
+namespace {
+
+typedef unsigned long long u64;
+typedef long long i64;
+
+// ---- bit-exact FP64 (reference operation order, every operation rounded) ----
+__device__ __forceinline__ double flux(double ksum, double ub, double ua) {
+  return __dmul_rn(ksum, __dsub_rn(ub, ua));
+}
+
+// base is u + rhs (or u alone when the problem has no source term: u + 0.0
+// equals u for every value but -0.0, which these fields never hold).
+__device__ __forceinline__ double combine(double base, double factor, double A, double B,
+                                          double C, double D, double E, double F) {
+  double s = __dsub_rn(__dadd_rn(__dsub_rn(__dadd_rn(__dsub_rn(A, B), C), D), E), F);
+  return __dadd_rn(base, __dmul_rn(factor, s));
+}
+
+template <bool RHS>
+__device__ __forceinline__ void walk_exact_faces(double *__restrict__ un,
+                                                 const double *__restrict__ u,
+                                                 const double *__restrict__ rhs,
+                                                 const double *__restrict__ kx,
+                                                 const double *__restrict__ ky,
+                                                 const double *__restrict__ kz, int P,
+                                                 size_t S, size_t c, int kb, int ke,
+                                                 double factor) {
+  double uc = u[c];
+  double F = flux(kz[c - S], uc, u[c - S]);
+  for (int k = kb; k < ke; ++k, c += S) {
+    double uu = u[c + S];
+    double A = flux(kx[c], u[c + 1], uc);
+    double B = flux(kx[c - 1], uc, u[c - 1]);
+    double C = flux(ky[c], u[c + P], uc);
+    double D = flux(ky[c - P], uc, u[c - P]);
+    double E = flux(kz[c], uu, uc);
+    un[c] = combine(RHS ? __dadd_rn(uc, rhs[c]) : uc, factor, A, B, C, D, E, F);
+    F = E;
+    uc = uu;
+  }
+}
+
+// ---- default FP64 form: integer pipes and FP64 pipe ----
+struct Dec {
+  int e;    // biased exponent, subnormals and zero mapped to 1
+  i64 m9;   // signed significand << 9  (|m9| < 2^62)
+};
+
+__device__ __forceinline__ Dec decode(u64 b) {
+  Dec d;
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  int ex = (int)((hi >> 20) & 0x7ffu);
+  const unsigned mh = (hi & 0xfffffu) | (ex ? 0x100000u : 0u);
+  d.e = max(ex, 1);
+  const u64 mag9 = ((((u64)mh) << 32) | lo) << 9;
+  d.m9 = ((int)hi < 0) ? -(i64)mag9 : (i64)mag9;
+  return d;
+}
+
+__device__ __forceinline__ i64 align(const Dec &d, int E) {
+  return d.m9 >> min(E - d.e, 63);
+}
+
+// acc += floor-ish(Dp * W / 2^64) for unsigned Dp, W < 2^63: the three
+// partial products that reach the high word (d1 w1, hi(d1 w0), hi(d0 w1));
+// the dropped terms are below 3 units of acc.
+__device__ __forceinline__ void mac_hi(u64 &acc, u64 Dp, u64 W) {
+  unsigned alo = (unsigned)acc, ahi = (unsigned)(acc >> 32);
+  const unsigned d0 = (unsigned)Dp, d1 = (unsigned)(Dp >> 32);
+  const unsigned w0 = (unsigned)W, w1 = (unsigned)(W >> 32);
+  asm("mad.lo.cc.u32 %0, %2, %4, %0;\n\t"
+      "madc.hi.u32   %1, %2, %4, %1;\n\t"
+      "mad.hi.cc.u32 %0, %2, %5, %0;\n\t"
+      "addc.u32      %1, %1, 0;\n\t"
+      "mad.hi.cc.u32 %0, %3, %4, %0;\n\t"
+      "addc.u32      %1, %1, 0;"
+      : "+r"(alo), "+r"(ahi)
+      : "r"(d1), "r"(d0), "r"(w1), "r"(w0));
+  acc = ((u64)ahi << 32) | alo;
+}
+
+// Round acc * 2^(E-1084) to the nearest FP64 value (ties to even).
+__device__ __forceinline__ double encode(i64 acc, int E) {
+  if (acc == 0) return 0.0;
+  const u64 s = acc < 0 ? 0x8000000000000000ull : 0ull;
+  const u64 mag = acc < 0 ? (u64)(-acc) : (u64)acc;
+  const int lz = __clzll((i64)mag);
+  const u64 norm = mag << lz;
+  const int be = E + 2 - lz;
+  if (be >= 1 && be < 2047) {
+    const u64 mant = norm >> 11, rem = norm & 0x7ffull;
+    const u64 up = (rem > 0x400ull) | ((rem == 0x400ull) & (mant & 1ull));
+    return __longlong_as_double((i64)(s | ((((u64)(be - 1)) << 52) + mant + up)));
+  }
+  return ldexp((double)acc, E - 1084);  // subnormal or overflowing result
+}
+
+__device__ __noinline__ double slow_point(double uc, double ue, double uw, double un, double us,
+                                          double uu, double ud, double r, u64 Kc, u64 Ke,
+                                          u64 Kw, u64 Kn, u64 Ks, u64 Ku, u64 Kd) {
+  const double s = 0x1p-64;
+  double acc = uc + r;
+  acc += (double)(Kc + Ke) * s * (ue - uc);
+  acc += (double)(Kc + Kw) * s * (uw - uc);
+  acc += (double)(Kc + Kn) * s * (un - uc);
+  acc += (double)(Kc + Ks) * s * (us - uc);
+  acc += (double)(Kc + Ku) * s * (uu - uc);
+  acc += (double)(Kc + Kd) * s * (ud - uc);
+  return acc;
+}
+
+constexpr u64 kSign = 0x8000000000000000ull;
+
+// The integer-pipe walk over one (i, j) column, planes [kb, ke).
+template <bool RHS>
+__device__ __forceinline__ void walk_int(double *__restrict__ un, const u64 *__restrict__ ub,
+                                         const double *__restrict__ rhs,
+                                         const u64 *__restrict__ K, int P, size_t S,
+                                         size_t c, int kb, int ke) {
+  u64 bd = ub[c - S], bc = ub[c];
+  Dec dd = decode(bd), dc = decode(bc);
+  u64 Kd = K[c - S], Kc = K[c];
+  // Loads of the next plane are issued one iteration ahead.
+  u64 nu = ub[c + S], ne = ub[c + 1], nw = ub[c - 1], nn = ub[c + P], ns = ub[c - P];
+  u64 mu = K[c + S], me = K[c + 1], mw = K[c - 1], mn = K[c + P], ms = K[c - P];
+  for (int k = kb; k < ke; ++k, c += S) {
+    const u64 bu = nu, be = ne, bw = nw, bn = nn, bs = ns;
+    const u64 Ku = mu, Ke = me, Kw = mw, Kn = mn, Ks = ms;
+    if (k + 1 < ke) {
+      const size_t q = c + S;
+      nu = ub[q + S]; ne = ub[q + 1]; nw = ub[q - 1]; nn = ub[q + P]; ns = ub[q - P];
+      mu = K[q + S]; me = K[q + 1]; mw = K[q - 1]; mn = K[q + P]; ms = K[q - P];
+    }
+    const Dec du = decode(bu), de = decode(be), dw = decode(bw), dn = decode(bn), ds = decode(bs);
+    int E = max(max(max(dc.e, du.e), max(dd.e, de.e)), max(max(dw.e, dn.e), ds.e));
+    Dec dr;
+    u64 br = 0;
+    if (RHS) {
+      br = __double_as_longlong(rhs[c]);
+      dr = decode(br);
+      E = max(E, dr.e);
+    }
+    double out;
+    if (E < 2047) {
+      const i64 Ac = align(dc, E);
+      const u64 We = Kc + Ke, Ww = Kc + Kw, Wn = Kc + Kn, Ws = Kc + Ks, Wu = Kc + Ku, Wd = Kc + Kd;
+      // Each product is taken of D + 2^63 (D = A_f - A_C, |D| < 2^63) so it is
+      // unsigned; the offsets sum to (sum_f W_f) / 2, removed up front.
+      u64 acc = (u64)Ac - ((We + Ww + Wn + Ws + Wu + Wd) >> 1);
+      mac_hi(acc, (u64)(align(de, E) - Ac) ^ kSign, We);
+      mac_hi(acc, (u64)(align(dw, E) - Ac) ^ kSign, Ww);
+      mac_hi(acc, (u64)(align(dn, E) - Ac) ^ kSign, Wn);
+      mac_hi(acc, (u64)(align(ds, E) - Ac) ^ kSign, Ws);
+      mac_hi(acc, (u64)(align(du, E) - Ac) ^ kSign, Wu);
+      mac_hi(acc, (u64)(align(dd, E) - Ac) ^ kSign, Wd);
+      if (RHS) acc += (u64)align(dr, E);
+      out = encode((i64)acc, E);
+    } else {
+      out = slow_point(__longlong_as_double(bc), __longlong_as_double(be), __longlong_as_double(bw),
+                       __longlong_as_double(bn), __longlong_as_double(bs),
+                       __longlong_as_double(bu), __longlong_as_double(bd),
+                       RHS ? __longlong_as_double(br) : 0.0, Kc, Ke, Kw, Kn, Ks, Ku, Kd);
+    }
+    un[c] = out;
+    bd = bc;
+    bc = bu;
+    dd = dc;
+    dc = du;
+    Kd = Kc;
+    Kc = Ku;
+  }
+}
+
+// The FP64-pipe walk (precomputed double weights, 7 FMA per point).
+template <bool RHS>
+__device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *__restrict__ u,
+                                        const double *__restrict__ rhs,
+                                        const double *__restrict__ c0,
+                                        const double *__restrict__ cx,
+                                        const double *__restrict__ cy,
+                                        const double *__restrict__ cz, int P, size_t S,
+                                        size_t c, int kb, int ke) {
+  double ud = u[c - S], uc = u[c];
+  double wd = cz[c - S];
+  for (int k = kb; k < ke; ++k, c += S) {
+    const double uu = u[c + S], wu = cz[c];
+    double acc = RHS ? fma(c0[c], uc, rhs[c]) : c0[c] * uc;
+    acc = fma(cx[c], u[c + 1], acc);
+    acc = fma(cx[c - 1], u[c - 1], acc);
+    acc = fma(cy[c], u[c + P], acc);
+    acc = fma(cy[c - P], u[c - P], acc);
+    acc = fma(wu, uu, acc);
+    acc = fma(wd, ud, acc);
+    un[c] = acc;
+    ud = uc;
+    uc = uu;
+    wd = wu;
+  }
+}
+
+// ---- FP32-compensated form ----
+__device__ __forceinline__ float bf2f(uint16_t b) {
+  return __uint_as_float(((unsigned)b) << 16);
+}
+__device__ __forceinline__ uint16_t f2bf(float x) {
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  return *reinterpret_cast<uint16_t *>(&h);
+}
+
+template <bool RHS>
+__device__ __forceinline__ void walk_fp32c(float *__restrict__ vn, uint16_t *__restrict__ cn,
+                                           const float *__restrict__ v,
+                                           const uint16_t *__restrict__ cr,
+                                           const float *__restrict__ wx,
+                                           const float *__restrict__ wy,
+                                           const float *__restrict__ wz,
+                                           const float *__restrict__ rhs, int P, size_t S,
+                                           size_t c, int kb, int ke) {
+  float vd = v[c - S], vc = v[c];
+  float wd = wz[c - S];
+  for (int k = kb; k < ke; ++k, c += S) {
+    const float vu = v[c + S], wu = wz[c];
+    float d = RHS ? rhs[c] : 0.0f;
+    d = fmaf(wx[c], v[c + 1] - vc, d);
+    d = fmaf(wx[c - 1], v[c - 1] - vc, d);
+    d = fmaf(wy[c], v[c + P] - vc, d);
+    d = fmaf(wy[c - P], v[c - P] - vc, d);
+    d = fmaf(wu, vu - vc, d);
+    d = fmaf(wd, vd - vc, d);
+    const float y = __fsub_rn(d, bf2f(cr[c]));
+    const float t = __fadd_rn(vc, y);
+    const float cc = __fsub_rn(__fsub_rn(t, vc), y);
+    vn[c] = t;
+    cn[c] = f2bf(cc);
+    vd = vc;
+    vc = vu;
+    wd = wu;
+  }
+}
+
+}  // namespace
+}  // namespace walk
+}  // namespace heat
