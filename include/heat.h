@@ -135,6 +135,43 @@ int heat_destroy(heat_ctx *c);
 
 const char *heat_strerror(int status);
 
+/* ---- batches: many grids advanced together over one tile table ---------- */
+
+/* No counterpart in the reference (it runs one grid per process).  A batch
+ * holds contexts of any size and form (HEAT_FP64 default or HEAT_BITEXACT,
+ * HEAT_FP32C; not HEAT_NAIVE) on one device.  heat_batch_run advances every
+ * context that still has scheduled steps by one step per launch of one kernel
+ * per kind present (form x source term), each walking a tile table over all
+ * grids of its kind; runs of 16 steps are captured once as a CUDA graph and
+ * replayed.  Per-context results are
+ * identical to heat_step on the context alone.  While a context is in a
+ * batch, step it through the batch (stepping it directly is detected and the
+ * batch rebuilds its table).                                                   */
+typedef struct heat_batch heat_batch;
+#define HEAT_BATCH_NO_GRAPHS     0x1u  /* plain launches only                  */
+#define HEAT_BATCH_PERSISTENT    0x2u  /* resident blocks stride the tile table */
+#define HEAT_BATCH_SERIAL_FORMS  0x4u  /* kinds one after another, one stream  */
+
+int heat_batch_create(heat_batch **out, void *stream, unsigned flags);
+/* Schedule `steps` more steps for c (adds c to the batch if new).            */
+int heat_batch_add(heat_batch *b, heat_ctx *c, long long steps);
+int heat_batch_remove(heat_batch *b, heat_ctx *c);
+int heat_batch_pending(heat_batch *b, heat_ctx *c, long long *steps_left);
+/* Run until every context's scheduled steps are done, or at most max_steps
+ * batch steps if max_steps >= 0.  Synchronises the batch's stream.           */
+int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken);
+int heat_batch_stats(heat_batch *b, long long *kernel_launches, long long *graph_launches,
+                     long long *batch_steps);
+int heat_batch_destroy(heat_batch *b);
+
+/* Autotune the batch kernel's z-chunk for one form (precision + HEAT_BITEXACT
+ * / HEAT_HWFP64 flags) over the size classes up to max_nz (<= 0: all), and
+ * write the JSON cache ($HEAT_TUNE_CACHE, else heat_tune.json beside the
+ * library).  Classes already cached are kept unless force != 0.              */
+int heat_tune_batch(int precision, unsigned flags, int max_nz, int force);
+/* z-chunk the batch kernel will use for a grid of depth nz.                   */
+int heat_tune_lookup(int precision, unsigned flags, int nz, int *kchunk);
+
 /* ---- drop-in for the reference's per-step device call -------------------- */
 
 /* Same signature and meaning as the reference's

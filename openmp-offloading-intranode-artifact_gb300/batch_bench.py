@@ -1,0 +1,103 @@
+"""Configuration 3: batched uneven grids in one persistent launch per step.
+
+    python openmp-offloading-intranode-artifact_gb300/batch_bench.py [--grids 64] [--seed 3]
+        [--min-axis 48] [--max-axis 384] [--min-steps 200] [--max-steps 2000] [--no-tune]
+
+64 independent solves; each axis drawn uniformly from {48..384}, kappa =
+exp(0.5 g) per grid (configuration-0 distributions, own seed), step counts
+uniform in [200, 2000], even-indexed grids FP64 (default form) and odd-indexed
+FP32C.  The batch kernel's z-chunks come from the autotuner (JSON cache; tuned
+here first unless --no-tune) and runs of 16 steps replay a CUDA graph.
+Prints one JSON line: aggregate GLUP/s of the batch (all updates of all grids
+over the device time of heat_batch_run, CUDA events), launches and graph
+launches, and for comparison the same grids advanced one context at a time
+with heat_step (the one-launch-per-step structure of the reference's loop).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import random
+import sys
+import time
+from pathlib import Path
+
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+import heat_ctypes as H  # noqa: E402
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--grids", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--min-axis", type=int, default=48)
+    ap.add_argument("--max-axis", type=int, default=384)
+    ap.add_argument("--min-steps", type=int, default=200)
+    ap.add_argument("--max-steps", type=int, default=2000)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--skip-sequential", action="store_true")
+    a = ap.parse_args()
+    import torch
+
+    rng = random.Random(a.seed)
+    specs = []
+    for g in range(a.grids):
+        shape = tuple(rng.randint(a.min_axis, a.max_axis) for _ in range(3))
+        specs.append({"shape": shape, "seed": 1000 * a.seed + g, "steps": rng.randint(a.min_steps, a.max_steps),
+                      "precision": H.HEAT_FP64 if g % 2 == 0 else H.HEAT_FP32C})
+    t0 = time.perf_counter()
+    if not a.no_tune:
+        H.tune_batch(H.HEAT_FP64, 0, max_nz=a.max_axis)
+        H.tune_batch(H.HEAT_FP32C, 0, max_nz=a.max_axis)
+    tune_s = time.perf_counter() - t0
+
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    solvers = []
+    for sp in specs:
+        nx, ny, nz = sp["shape"]
+        kappa, u0, h, dt = H.inputs_config(0, sp["seed"], nx, ny, nz)
+        solvers.append(H.Solver(kappa, u0, h, dt, precision=sp["precision"], stream=stream.cuda_stream))
+    setup_s = time.perf_counter() - t0
+    updates = sum((sp["shape"][0] - 2) * (sp["shape"][1] - 2) * (sp["shape"][2] - 2) * sp["steps"]
+                  for sp in specs)
+
+    batch = H.Batch(stream=stream.cuda_stream)
+    for s, sp in zip(solvers, specs):
+        batch.add(s, sp["steps"])
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    taken = batch.run()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches, graphs, _ = batch.stats()
+    batch.close()
+    out = {"workload": f"config3: {a.grids} grids, axes U{{{a.min_axis}..{a.max_axis}}}, steps "
+                       f"U[{a.min_steps},{a.max_steps}], half FP64 / half FP32C",
+           "updates": updates, "batch_ms": round(ms, 2), "batch_glups": round(updates / (ms * 1e-3) / 1e9, 2),
+           "batch_steps": taken, "kernel_launches": launches, "graph_launches": graphs,
+           "tune_s": round(tune_s, 2), "setup_s": round(setup_s, 2),
+           "kchunks": {str(n): H.tune_lookup(p, 0, n) for p in (0, 1) for n in (64, 128, 256, 384)}}
+    if not a.skip_sequential:
+        # the same work, one context at a time with heat_step (fresh contexts)
+        seq_ms = 0.0
+        for sp in specs:
+            nx, ny, nz = sp["shape"]
+            kappa, u0, h, dt = H.inputs_config(0, sp["seed"], nx, ny, nz)
+            with H.Solver(kappa, u0, h, dt, precision=sp["precision"], stream=stream.cuda_stream) as s:
+                f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                f0.record(stream)
+                s.step(sp["steps"])
+                f1.record(stream)
+                f1.synchronize()
+                seq_ms += f0.elapsed_time(f1)
+        out["sequential_ms"] = round(seq_ms, 2)
+        out["sequential_glups"] = round(updates / (seq_ms * 1e-3) / 1e9, 2)
+    for s in solvers:
+        s.close()
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,492 @@
+// heat_batch_*: many contexts advanced together by one launch per kernel kind
+// per time step over a shared tile table (heat_batch.cu), with runs of steps
+// captured once as a CUDA graph and replayed.  Host code only.
+//
+// Launch shape: by default one block per tile, scheduled by the hardware; with
+// HEAT_BATCH_PERSISTENT a fixed set of resident blocks strides the table
+// instead.  On configuration 3 (64 uneven grids, half FP64, half FP32C) the
+// hardware-scheduled shape measured 92 GLUP/s against 86 for the persistent
+// one, whose blocks serialise each tile's start-up loads.  Kinds (form x
+// source term) present together run on their own streams, forked from and
+// joined to the batch stream, unless HEAT_BATCH_SERIAL_FORMS.
+//
+// Bookkeeping: every active context advances one step per launch; the device
+// table records each grid's current buffer at build time and each launch gets
+// the parity of the steps taken since, so a graph of an even number of steps
+// can be replayed any number of times.  The table is rebuilt (and the graph
+// re-captured) only when the set of active contexts changes.
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <new>
+#include <vector>
+
+#include "heat_batch_internal.h"
+
+struct heat_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  unsigned flags = 0;
+  int kchunk_override = 0;
+
+  struct Entry {
+    heat_ctx *ctx;
+    long long remaining;
+    long long base_steps;  // ctx->steps_done when the table was built
+  };
+  std::vector<Entry> entries;
+  std::vector<int> active;  // entry indices in table order
+
+  heat::BatchGrid *d_grids = nullptr;
+  size_t cap_grids = 0;
+  heat::BatchTile *d_tiles = nullptr;
+  size_t cap_tiles = 0;
+  int ntiles = 0;
+  // Tiles are grouped by form: form f owns [tile_begin[f], tile_begin[f] + tile_count[f]).
+  int tile_begin[heat::kNumKinds] = {};
+  int tile_count[heat::kNumKinds] = {};
+  int form_blocks[heat::kNumKinds] = {};
+  int nforms = 0;
+  // Side streams and events for running the forms' kernels side by side.
+  cudaStream_t side[heat::kNumKinds] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[heat::kNumKinds] = {};
+  bool dirty = true;
+  long long since_build = 0;
+
+  cudaGraphExec_t gexec = nullptr;
+  int graph_parity = -1;
+  int graph_steps = 16;  // even
+
+  int blocks_per_sm[heat::kNumKinds] = {};
+  int sms = 0;
+  bool persistent = false;  // resident blocks stride the tile table (HEAT_BATCH_PERSISTENT)
+  bool concurrent = true;   // forms run side by side on their own streams
+  long long launches = 0, graph_launches = 0, batch_steps = 0;
+};
+
+namespace heat {
+
+int batch_form(const heat_ctx *c) {
+  if (c->precision == HEAT_FP32C) return kFormF32c;
+  if (c->flags & HEAT_NAIVE) return -1;
+  if (c->flags & HEAT_BITEXACT) return kFormExact;
+  return c->kq ? kFormMix : kFormHw;
+}
+
+void batch_set_kchunk_override(heat_batch *b, int kchunk) {
+  b->kchunk_override = kchunk;
+  b->dirty = true;
+}
+
+}  // namespace heat
+
+namespace {
+
+void drop_graph(heat_batch *b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->graph_parity = -1;
+}
+
+void release(heat_batch *b) {
+  drop_graph(b);
+  for (int f = 0; f < heat::kNumKinds; ++f) {
+    if (b->side[f]) {
+      cudaStreamSynchronize(b->side[f]);
+      cudaStreamDestroy(b->side[f]);
+    }
+    if (b->join_ev[f]) cudaEventDestroy(b->join_ev[f]);
+  }
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  if (b->d_grids) cudaFree(b->d_grids);
+  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+template <class T>
+int grow(T **p, size_t *cap, size_t need) {
+  if (need <= *cap) return HEAT_OK;
+  size_t n = std::max(need, *cap * 2);
+  T *q = nullptr;
+  if (cudaMalloc((void **)&q, n * sizeof(T)) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ENOMEM;
+  }
+  if (*p) cudaFree(*p);
+  *p = q;
+  *cap = n;
+  return HEAT_OK;
+}
+
+bool grid_has_rhs(const heat_ctx *c) {
+  return c->precision == HEAT_FP32C ? c->frhs != nullptr : c->rhs != nullptr;
+}
+
+heat::BatchGrid describe(const heat_ctx *c, int form) {
+  heat::BatchGrid g{};
+  g.form = form;
+  g.nx = c->g.nx;
+  g.ny = c->g.ny;
+  g.nz = c->g.nz;
+  g.P = c->g.pitch;
+  g.S = c->g.plane;
+  g.factor = c->factor;
+  g.cur = c->cur;
+  g.hw_rows = c->hw_rows;
+  if (form == heat::kFormF32c) {
+    g.f[0] = c->v[0];
+    g.f[1] = c->v[1];
+    g.cr[0] = c->carry[0];
+    g.cr[1] = c->carry[1];
+    g.rhs = c->frhs;
+    for (int a = 0; a < 3; ++a) g.w[a] = c->fcf[a];
+  } else {
+    g.f[0] = c->u[0];
+    g.f[1] = c->u[1];
+    g.rhs = c->rhs;
+    if (form == heat::kFormExact) {
+      for (int a = 0; a < 3; ++a) g.w[a] = c->ks[a];
+    } else {
+      g.w[0] = c->c0;
+      for (int a = 0; a < 3; ++a) g.w[a + 1] = c->cf[a];
+      g.kq = c->kq;
+      if (form == heat::kFormHw) g.hw_rows = 8;
+    }
+  }
+  return g;
+}
+
+// Throughput guesses (GLUP/s on GB300) used only to split the SMs between
+// forms that run side by side.
+const double kFormRate[heat::kNumForms] = {90.0, 80.0, 29.0, 200.0};
+
+int rebuild(heat_batch *b) {
+  drop_graph(b);
+  b->active.clear();
+  std::vector<heat::BatchGrid> grids;
+  std::vector<heat::BatchTile> per_form[heat::kNumKinds];
+  double work[heat::kNumKinds] = {};
+  for (size_t e = 0; e < b->entries.size(); ++e) {
+    const heat_batch::Entry &en = b->entries[e];
+    if (en.remaining <= 0) continue;
+    const heat_ctx *c = en.ctx;
+    b->entries[e].base_steps = c->steps_done;
+    const int form = heat::batch_form(c);
+    const int kind = 2 * form + (grid_has_rhs(c) ? 1 : 0);
+    const int gi = (int)grids.size();
+    grids.push_back(describe(c, form));
+    b->active.push_back((int)e);
+    const int interior = c->g.nz - 2;
+    int kc = b->kchunk_override > 0 ? b->kchunk_override : heat::tuned_kchunk(form, c->g.nz);
+    kc = std::max(1, std::min(kc, interior));
+    const int ntx = (c->g.nx - 2 + 31) / 32, nty = (c->g.ny - 2 + 7) / 8;
+    for (int k0 = 1; k0 < c->g.nz - 1; k0 += kc) {
+      const int k1 = std::min(k0 + kc, c->g.nz - 1);
+      for (int ty = 0; ty < nty; ++ty)
+        for (int tx = 0; tx < ntx; ++tx) per_form[kind].push_back({gi, tx, ty, k0, k1});
+    }
+    work[kind] += (double)(c->g.nx - 2) * (c->g.ny - 2) * interior / kFormRate[form];
+  }
+  std::vector<heat::BatchTile> tiles;
+  double total = 0;
+  b->nforms = 0;
+  for (int f = 0; f < heat::kNumKinds; ++f) {
+    b->tile_begin[f] = (int)tiles.size();
+    b->tile_count[f] = (int)per_form[f].size();
+    tiles.insert(tiles.end(), per_form[f].begin(), per_form[f].end());
+    total += work[f];
+    if (b->tile_count[f] > 0) ++b->nforms;
+  }
+  // Resident blocks per form: the whole GPU for a lone form; with several
+  // forms, each gets SMs in proportion to its estimated time so they finish
+  // together while sharing every SM.
+  for (int f = 0; f < heat::kNumKinds; ++f) {
+    if (b->tile_count[f] == 0) {
+      b->form_blocks[f] = 0;
+      continue;
+    }
+    if (!b->persistent) {
+      b->form_blocks[f] = b->tile_count[f];  // one tile per block, hardware-scheduled
+      continue;
+    }
+    const double share = (b->nforms == 1 || total <= 0 || !b->concurrent) ? 1.0 : work[f] / total;
+    long long full = (long long)b->blocks_per_sm[f] * b->sms;
+    long long nb = std::max(1LL, (long long)(share * full + 0.5));
+    b->form_blocks[f] = (int)std::min<long long>(nb, b->tile_count[f]);
+  }
+  int rc = grow(&b->d_grids, &b->cap_grids, std::max<size_t>(1, grids.size()));
+  if (rc == HEAT_OK) rc = grow(&b->d_tiles, &b->cap_tiles, std::max<size_t>(1, tiles.size()));
+  if (rc != HEAT_OK) return rc;
+  if (!grids.empty() &&
+      (cudaMemcpyAsync(b->d_grids, grids.data(), grids.size() * sizeof(heat::BatchGrid),
+                       cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+       cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(heat::BatchTile),
+                       cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+       cudaStreamSynchronize(b->stream) != cudaSuccess)) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  b->ntiles = (int)tiles.size();
+  b->since_build = 0;
+  b->dirty = false;
+  return HEAT_OK;
+}
+
+// Account n steps for every active context.
+void advance(heat_batch *b, long long n) {
+  for (int e : b->active) {
+    heat_batch::Entry &en = b->entries[e];
+    en.ctx->steps_done += n;
+    if (n & 1) en.ctx->cur ^= 1;
+    en.remaining -= n;
+  }
+  b->since_build += n;
+  b->batch_steps += n;
+}
+
+// Enqueue `n` steps starting at parity p: each form's kernel on its own side
+// stream (forked from and joined back to the batch stream) when several forms
+// are present, so a memory-bound and a compute-bound form share the SMs.
+cudaError_t enqueue_steps(heat_batch *b, int p, int n) {
+  cudaError_t err = cudaSuccess;
+  if (b->nforms <= 1 || !b->concurrent) {
+    for (int f = 0; f < heat::kNumKinds; ++f) {
+      if (!b->tile_count[f]) continue;
+      for (int s = 0; s < n && err == cudaSuccess; ++s)
+        err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
+                                 (p + s) & 1, b->form_blocks[f], b->stream);
+    }
+    return err;
+  }
+  err = cudaEventRecord(b->fork_ev, b->stream);
+  for (int f = 0; f < heat::kNumKinds && err == cudaSuccess; ++f) {
+    if (!b->tile_count[f]) continue;
+    err = cudaStreamWaitEvent(b->side[f], b->fork_ev, 0);
+    for (int s = 0; s < n && err == cudaSuccess; ++s)
+      err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
+                               (p + s) & 1, b->form_blocks[f], b->side[f]);
+    if (err == cudaSuccess) err = cudaEventRecord(b->join_ev[f], b->side[f]);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(b->stream, b->join_ev[f], 0);
+  }
+  return err;
+}
+
+int launch_plain(heat_batch *b, int n) {
+  if (enqueue_steps(b, (int)(b->since_build & 1), n) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  b->launches += (long long)n * b->nforms;
+  advance(b, n);
+  return HEAT_OK;
+}
+
+int capture_graph(heat_batch *b) {
+  drop_graph(b);
+  cudaGraph_t graph = nullptr;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  const int p = (int)(b->since_build & 1);
+  cudaError_t err = enqueue_steps(b, p, b->graph_steps);
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+  if (err != cudaSuccess || e2 != cudaSuccess || !graph) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  cudaError_t e3 = cudaGraphInstantiate(&b->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e3 != cudaSuccess) {
+    b->gexec = nullptr;
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  b->graph_parity = p;
+  return HEAT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int heat_batch_create(heat_batch **out, void *stream, unsigned flags) {
+  if (!out) return HEAT_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return HEAT_ENODEV;
+  }
+  heat_batch *b = new (std::nothrow) heat_batch();
+  if (!b) return HEAT_ENOMEM;
+  b->flags = flags;
+  cudaGetDevice(&b->device);
+  cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
+  for (int f = 0; f < heat::kNumKinds; ++f) b->blocks_per_sm[f] = heat::batch_blocks_per_sm(f);
+  b->persistent = (flags & HEAT_BATCH_PERSISTENT) != 0;
+  b->concurrent = (flags & HEAT_BATCH_SERIAL_FORMS) == 0;
+  bool ok = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  for (int f = 0; f < heat::kNumKinds && ok; ++f)
+    ok = cudaStreamCreateWithFlags(&b->side[f], cudaStreamNonBlocking) == cudaSuccess &&
+         cudaEventCreateWithFlags(&b->join_ev[f], cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    release(b);
+    return HEAT_ECUDA;
+  }
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+  } else {
+    // Graph capture needs a stream other than the legacy default one.
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      cudaGetLastError();
+      delete b;
+      return HEAT_ECUDA;
+    }
+    b->own_stream = true;
+  }
+  *out = b;
+  return HEAT_OK;
+}
+
+int heat_batch_add(heat_batch *b, heat_ctx *c, long long steps) {
+  if (!b || !c || steps < 0) return HEAT_EINVAL;
+  if (c->device != b->device || heat::batch_form(c) < 0) return HEAT_EINVAL;
+  for (auto &en : b->entries)
+    if (en.ctx == c) {
+      if (en.remaining <= 0 && steps > 0) b->dirty = true;
+      en.remaining += steps;
+      return HEAT_OK;
+    }
+  // Work already queued on the context's own stream finishes first.
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  b->entries.push_back({c, steps, c->steps_done});
+  if (steps > 0) b->dirty = true;
+  return HEAT_OK;
+}
+
+int heat_batch_remove(heat_batch *b, heat_ctx *c) {
+  if (!b || !c) return HEAT_EINVAL;
+  for (size_t e = 0; e < b->entries.size(); ++e)
+    if (b->entries[e].ctx == c) {
+      if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return HEAT_ECUDA;
+      }
+      b->entries.erase(b->entries.begin() + (long)e);
+      b->dirty = true;
+      return HEAT_OK;
+    }
+  return HEAT_EINVAL;
+}
+
+int heat_batch_pending(heat_batch *b, heat_ctx *c, long long *steps_left) {
+  if (!b || !c) return HEAT_EINVAL;
+  for (auto &en : b->entries)
+    if (en.ctx == c) {
+      if (steps_left) *steps_left = en.remaining > 0 ? en.remaining : 0;
+      return HEAT_OK;
+    }
+  return HEAT_EINVAL;
+}
+
+int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken) {
+  if (!b) return HEAT_EINVAL;
+  long long done = 0;
+  int rc = HEAT_OK;
+  // Work queued on the member contexts' own streams (e.g. steps taken outside
+  // the batch) finishes first; a context stepped outside the batch since the
+  // table was built has moved its current buffer, so the table is rebuilt.
+  for (auto &en : b->entries)
+    if (cudaStreamSynchronize(en.ctx->stream) != cudaSuccess) {
+      cudaGetLastError();
+      return HEAT_ECUDA;
+    }
+  for (int e : b->active)
+    if (b->entries[e].ctx->steps_done != b->entries[e].base_steps + b->since_build) b->dirty = true;
+  for (;;) {
+    if (b->dirty) {
+      rc = rebuild(b);
+      if (rc != HEAT_OK) break;
+    }
+    if (b->active.empty()) break;
+    long long m = -1;
+    for (int e : b->active) {
+      long long r = b->entries[e].remaining;
+      if (m < 0 || r < m) m = r;
+    }
+    if (max_steps >= 0) m = std::min(m, max_steps - done);
+    if (m <= 0) break;
+    const bool graphs = !(b->flags & HEAT_BATCH_NO_GRAPHS);
+    if (graphs && m >= b->graph_steps) {
+      if (b->gexec && b->graph_parity != (int)(b->since_build & 1)) {
+        // the graph was captured at the other parity: one plain launch first
+        rc = launch_plain(b, 1);
+        if (rc != HEAT_OK) break;
+        ++done;
+        --m;
+      }
+      if (m >= b->graph_steps) {
+        if (!b->gexec) {
+          rc = capture_graph(b);
+          if (rc != HEAT_OK) break;
+        }
+        const long long reps = m / b->graph_steps;
+        for (long long r = 0; r < reps; ++r) {
+          if (cudaGraphLaunch(b->gexec, b->stream) != cudaSuccess) {
+            cudaGetLastError();
+            rc = HEAT_ECUDA;
+            break;
+          }
+          b->graph_launches += 1;
+          b->launches += (long long)b->graph_steps * b->nforms;
+          advance(b, b->graph_steps);
+          done += b->graph_steps;
+        }
+        if (rc != HEAT_OK) break;
+        m -= reps * b->graph_steps;
+      }
+    }
+    if (m > 0) {
+      rc = launch_plain(b, (int)m);
+      if (rc != HEAT_OK) break;
+      done += m;
+    }
+    for (int e : b->active)
+      if (b->entries[e].remaining <= 0) b->dirty = true;
+    if (max_steps >= 0 && done >= max_steps) break;
+  }
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+    cudaGetLastError();
+    if (rc == HEAT_OK) rc = HEAT_ECUDA;
+  }
+  if (steps_taken) *steps_taken = done;
+  return rc;
+}
+
+int heat_batch_stats(heat_batch *b, long long *kernel_launches, long long *graph_launches,
+                     long long *batch_steps) {
+  if (!b) return HEAT_EINVAL;
+  if (kernel_launches) *kernel_launches = b->launches;
+  if (graph_launches) *graph_launches = b->graph_launches;
+  if (batch_steps) *batch_steps = b->batch_steps;
+  return HEAT_OK;
+}
+
+int heat_batch_destroy(heat_batch *b) {
+  if (!b) return HEAT_EINVAL;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  release(b);
+  return HEAT_OK;
+}
+
+}  // extern "C"

@@ -264,16 +264,39 @@ __device__ __forceinline__ void walk_fp32c(float *__restrict__ vn, uint16_t *__r
                                            size_t c, int kb, int ke) {
   float vd = v[c - S], vc = v[c];
   float wd = wz[c - S];
+  // The plane's loads are issued one iteration ahead (the walk is bound by
+  // memory latency, not arithmetic).
+  float nu = v[c + S], nwz = wz[c], ne = v[c + 1], nw = v[c - 1], nn = v[c + P], ns = v[c - P];
+  float nwx = wx[c], nwxm = wx[c - 1], nwy = wy[c], nwym = wy[c - P];
+  uint16_t ncr = cr[c];
+  float nr = RHS ? rhs[c] : 0.0f;
   for (int k = kb; k < ke; ++k, c += S) {
-    const float vu = v[c + S], wu = wz[c];
-    float d = RHS ? rhs[c] : 0.0f;
-    d = fmaf(wx[c], v[c + 1] - vc, d);
-    d = fmaf(wx[c - 1], v[c - 1] - vc, d);
-    d = fmaf(wy[c], v[c + P] - vc, d);
-    d = fmaf(wy[c - P], v[c - P] - vc, d);
+    const float vu = nu, wu = nwz, ve = ne, vw = nw, vn_ = nn, vs = ns;
+    const float w_e = nwx, w_w = nwxm, w_n = nwy, w_s = nwym, r = nr;
+    const uint16_t cc0 = ncr;
+    if (k + 1 < ke) {
+      const size_t q = c + S;
+      nu = v[q + S];
+      nwz = wz[q];
+      ne = v[q + 1];
+      nw = v[q - 1];
+      nn = v[q + P];
+      ns = v[q - P];
+      nwx = wx[q];
+      nwxm = wx[q - 1];
+      nwy = wy[q];
+      nwym = wy[q - P];
+      ncr = cr[q];
+      if (RHS) nr = rhs[q];
+    }
+    float d = r;
+    d = fmaf(w_e, ve - vc, d);
+    d = fmaf(w_w, vw - vc, d);
+    d = fmaf(w_n, vn_ - vc, d);
+    d = fmaf(w_s, vs - vc, d);
     d = fmaf(wu, vu - vc, d);
     d = fmaf(wd, vd - vc, d);
-    const float y = __fsub_rn(d, bf2f(cr[c]));
+    const float y = __fsub_rn(d, bf2f(cc0));
     const float t = __fadd_rn(vc, y);
     const float cc = __fsub_rn(__fsub_rn(t, vc), y);
     vn[c] = t;

@@ -62,11 +62,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     headers = list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
     jobs = []
     for src in sorted(CSRC.glob("*.cu")):
-        obj = OBJ / (src.stem + ".o")
+        obj = OBJ / (src.name + ".o")
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc, *NVCC_COMMON, *UNIT_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)])
     for src in sorted(CSRC.glob("*.cpp")):
-        obj = OBJ / (src.stem + ".o")
+        obj = OBJ / (src.name + ".o")
         if force or _stale(obj, [src] + headers):
             jobs.append(["g++", "-O3", "-fPIC", "-std=c++17", "-ffp-contract=off", "-pthread",
                          "-I", str(ROOT / "include"), "-I", str(CSRC), "-I", str(_cuda_include(nvcc)),
@@ -77,7 +77,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
                 f.result()
     objs = sorted(OBJ.glob("*.o"))
     if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread"])
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lpthread", "-ldl"])
     drv_src = PKG / "driver" / "heatdrv.c"
     if drv_src.exists() and (force or _stale(DRV, [drv_src, LIB, ROOT / "include" / "heat.h"])):
         _run(["gcc", "-O2", "-std=c11", "-D_DEFAULT_SOURCE", "-I", str(ROOT / "include"),

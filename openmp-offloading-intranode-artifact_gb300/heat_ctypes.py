@@ -33,6 +33,10 @@ HEAT_BITEXACT = 0x1
 HEAT_NAIVE = 0x2
 HEAT_HWFP64 = 0x4
 
+HEAT_BATCH_NO_GRAPHS = 0x1
+HEAT_BATCH_PERSISTENT = 0x2
+HEAT_BATCH_SERIAL_FORMS = 0x4
+
 
 class HeatError(RuntimeError):
     def __init__(self, what: str, status: int, msg: str):
@@ -69,6 +73,16 @@ SIGNATURES = {
     "heat_update_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_int, C.c_int, C.c_int, C.c_double, C.c_void_p]),
     "heat_norm_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_void_p]),
+    "heat_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_void_p, C.c_uint]),
+    "heat_batch_add": (C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    "heat_batch_remove": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "heat_batch_pending": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_longlong)]),
+    "heat_batch_run": (C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_longlong)]),
+    "heat_batch_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                                   C.POINTER(C.c_longlong)]),
+    "heat_batch_destroy": (C.c_int, [C.c_void_p]),
+    "heat_tune_batch": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.c_int]),
+    "heat_tune_lookup": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.POINTER(C.c_int)]),
     "heat_inputs_reference": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _dp, _dp]),
     "heat_inputs_config": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int,
                                      C.c_void_p, C.c_void_p, _dp, _dp]),
@@ -207,3 +221,60 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class Batch:
+    """heat_batch: contexts advanced together by one persistent launch per step."""
+
+    def __init__(self, stream: int | None = None, graphs: bool = True, flags: int = 0):
+        self._b = C.c_void_p()
+        fl = flags | (0 if graphs else HEAT_BATCH_NO_GRAPHS)
+        check(lib().heat_batch_create(C.byref(self._b), stream, fl), "heat_batch_create")
+
+    def add(self, solver: Solver, steps: int) -> None:
+        check(lib().heat_batch_add(self._b, solver._ctx, steps), "heat_batch_add")
+
+    def remove(self, solver: Solver) -> None:
+        check(lib().heat_batch_remove(self._b, solver._ctx), "heat_batch_remove")
+
+    def pending(self, solver: Solver) -> int:
+        n = C.c_longlong()
+        check(lib().heat_batch_pending(self._b, solver._ctx, C.byref(n)), "heat_batch_pending")
+        return n.value
+
+    def run(self, max_steps: int = -1) -> int:
+        n = C.c_longlong()
+        check(lib().heat_batch_run(self._b, max_steps, C.byref(n)), "heat_batch_run")
+        return n.value
+
+    def stats(self) -> tuple[int, int, int]:
+        a, g, s = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        check(lib().heat_batch_stats(self._b, C.byref(a), C.byref(g), C.byref(s)), "heat_batch_stats")
+        return a.value, g.value, s.value
+
+    def close(self) -> None:
+        if self._b:
+            lib().heat_batch_destroy(self._b)
+            self._b = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tune_batch(precision: int = HEAT_FP64, flags: int = 0, max_nz: int = 0, force: bool = False) -> None:
+    check(lib().heat_tune_batch(precision, flags, max_nz, int(force)), "heat_tune_batch")
+
+
+def tune_lookup(precision: int, flags: int, nz: int) -> int:
+    k = C.c_int()
+    check(lib().heat_tune_lookup(precision, flags, nz, C.byref(k)), "heat_tune_lookup")
+    return k.value
