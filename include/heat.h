@@ -172,6 +172,56 @@ int heat_tune_batch(int precision, unsigned flags, int max_nz, int force);
 /* z-chunk the batch kernel will use for a grid of depth nz.                   */
 int heat_tune_lookup(int precision, unsigned flags, int nz, int *kchunk);
 
+/* ---- continuous-batching solve server ------------------------------------ */
+
+/* No counterpart in the reference.  A server owns one GPU worker thread and
+ * `prep_threads` input-generation threads.  Submitted requests get seeded
+ * synthetic inputs (heat_inputs_config), are admitted in arrival order while
+ * their device bytes fit `budget_bytes` (a request that does not fit waits;
+ * the next few behind it may go first), stay device-resident until done, and
+ * advance together through a heat_batch in ticks of `tick_steps` steps; new
+ * requests join at the next tick as memory frees up.  A request larger than
+ * the whole budget completes with status HEAT_EBUDGET.                       */
+typedef struct heat_server heat_server;
+
+typedef struct heat_request {
+  int nx, ny, nz;          /* points per axis, each >= 3                      */
+  long long steps;         /* explicit steps to take                          */
+  int precision;           /* HEAT_FP64 (default form) | HEAT_FP32C           */
+  int cfg;                 /* input distribution, as heat_inputs_config       */
+  uint64_t seed;
+  double *field_out;       /* optional host nz*ny*nx buffer for the final field,
+                              valid until the request's result is polled      */
+} heat_request;
+
+typedef struct heat_result {
+  uint64_t id;
+  int status;              /* HEAT_OK, HEAT_EBUDGET, ...                      */
+  double l2, checksum;     /* heat_norm of the final field                    */
+  double submit_ms, admit_ms, done_ms;  /* since the server was created      */
+  double updates;          /* interior points x steps                         */
+} heat_result;
+
+typedef struct heat_server_summary {
+  long long submitted, admitted, completed, rejected, resident, queued;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit-to-done latency         */
+  double glups;            /* completed updates / (last done - first admit)   */
+  double updates, busy_ms;
+  size_t budget_bytes, bytes_in_use, peak_bytes;
+  long long batch_steps, kernel_launches;
+} heat_server_summary;
+
+int heat_server_create(heat_server **out, size_t budget_bytes, int tick_steps, int prep_threads);
+/* Thread-safe; returns at once with the request's id.                         */
+int heat_server_submit(heat_server *s, const heat_request *r, uint64_t *id_out);
+/* Move up to max finished results into out; *n_out = how many.               */
+int heat_server_poll(heat_server *s, heat_result *out, int max, int *n_out);
+/* Block until every submitted request has finished.                           */
+int heat_server_wait_idle(heat_server *s);
+int heat_server_stats(heat_server *s, heat_server_summary *st);
+/* Stop: requests not yet admitted are dropped, resident ones finish.         */
+int heat_server_destroy(heat_server *s);
+
 /* ---- drop-in for the reference's per-step device call -------------------- */
 
 /* Same signature and meaning as the reference's

@@ -1,0 +1,431 @@
+// heat_server_*: a continuous-batching solve server on one GPU.
+//
+// Requests (grid size, step count, precision, seeded inputs) are submitted from
+// any thread.  Prep threads generate each request's host inputs off the GPU
+// path.  One GPU worker thread runs the loop
+//
+//   admit:   take prepared requests in arrival order while their device bytes
+//            fit the HBM budget (a request that does not fit waits; the next
+//            few behind it may be admitted first if they fit), create their
+//            contexts (fields stay device-resident until they finish) and add
+//            them to the batch with their step counts;
+//   advance: heat_batch_run for at most `tick_steps` batch steps -- every
+//            resident solve advances together, whatever its size and form;
+//   retire:  solves with no steps left report their norm (and field, if asked),
+//            release their memory and budget, and become results.
+//
+// so requests arriving while others are on the GPU join at the next tick as
+// memory frees up, and their work overlaps on the device.  Latency of a
+// request = completion time - submission time.
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <vector>
+
+#include "heat_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Job {
+  uint64_t id = 0;
+  heat_request req{};
+  double submit_ms = 0, admit_ms = 0;
+  size_t bytes = 0;
+  std::vector<double> kappa, u0;
+  double h = 0, dt = 0;
+  int status = HEAT_OK;
+  heat_ctx *ctx = nullptr;
+};
+
+// Device bytes a request holds while resident (fields, coefficient planes,
+// and the FP64 staging buffer heat_init uses), pitch padding included.
+size_t request_bytes(const heat_request &r) {
+  const size_t pitch = ((size_t)r.nx + 3) & ~(size_t)3;
+  const size_t pts = pitch * (size_t)r.ny * (size_t)r.nz;
+  return pts * (r.precision == HEAT_FP32C ? 32 : 64) + (1u << 20);
+}
+
+}  // namespace
+
+struct heat_server {
+  size_t budget = 0;
+  size_t prep_cap = 0;  // host bytes of prepared inputs held ahead of admission
+  int tick_steps = 64;
+  Clock::time_point t0;
+
+  std::mutex mu;
+  std::condition_variable cv_prep, cv_work, cv_idle;
+  std::deque<Job *> submitted;   // waiting for input generation
+  std::deque<Job *> ready;       // inputs generated, waiting for admission
+  std::vector<Job *> resident;   // on the GPU
+  std::vector<heat_result> done; // not yet polled
+  std::vector<double> latencies;
+  uint64_t next_id = 1;
+  bool stop = false;
+  int preparing = 0;
+
+  size_t in_use = 0, peak = 0, ready_bytes = 0;
+  long long n_submitted = 0, n_admitted = 0, n_completed = 0, n_rejected = 0;
+  double updates_done = 0;
+  double busy_ms = 0;            // wall time the worker spent advancing solves
+  double first_admit_ms = -1, last_done_ms = 0;
+
+  heat_batch *batch = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  std::vector<std::thread> preps;
+  std::thread worker;
+  int worker_status = HEAT_OK;
+};
+
+namespace {
+
+double now_ms(const heat_server *s) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - s->t0).count();
+}
+
+void finish(heat_server *s, Job *j, int status, double l2, double cs) {
+  heat_result r{};
+  r.id = j->id;
+  r.status = status;
+  r.l2 = l2;
+  r.checksum = cs;
+  r.submit_ms = j->submit_ms;
+  r.admit_ms = j->admit_ms;
+  r.done_ms = now_ms(s);
+  r.updates = status == HEAT_OK ? (double)(j->req.nx - 2) * (j->req.ny - 2) * (j->req.nz - 2) *
+                                      (double)j->req.steps
+                                : 0.0;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->done.push_back(r);
+  if (status == HEAT_OK) {
+    s->n_completed += 1;
+    s->latencies.push_back(r.done_ms - r.submit_ms);
+    s->updates_done += r.updates;
+    s->last_done_ms = r.done_ms;
+  } else {
+    s->n_rejected += 1;
+  }
+  s->cv_idle.notify_all();
+}
+
+void prep_loop(heat_server *s) {
+  for (;;) {
+    Job *j = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      // Bound host memory held by prepared inputs (look-ahead of the queue).
+      s->cv_prep.wait(lk, [&] {
+        return s->stop || (!s->submitted.empty() && s->ready_bytes < s->prep_cap);
+      });
+      if (s->stop) return;
+      j = s->submitted.front();
+      s->submitted.pop_front();
+      s->preparing += 1;
+    }
+    const heat_request &r = j->req;
+    const size_t n = (size_t)r.nx * r.ny * r.nz;
+    int rc = HEAT_OK;
+    try {
+      j->kappa.resize(n);
+      j->u0.resize(n);
+    } catch (...) {
+      rc = HEAT_ENOMEM;
+    }
+    if (rc == HEAT_OK)
+      rc = heat_inputs_config(r.cfg, r.seed, r.nx, r.ny, r.nz, j->kappa.data(), j->u0.data(),
+                              &j->h, &j->dt);
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->preparing -= 1;
+      if (rc == HEAT_OK) {
+        s->ready.push_back(j);
+        s->ready_bytes += n * 16;
+        s->cv_work.notify_one();
+      }
+    }
+    if (rc != HEAT_OK) {
+      finish(s, j, rc, 0, 0);
+      delete j;
+    }
+  }
+}
+
+// Admit prepared jobs that fit; returns the number admitted.
+int admit(heat_server *s) {
+  std::vector<Job *> take;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    const int window = 8;  // how far past a blocked head the scan looks
+    int looked = 0;
+    for (auto it = s->ready.begin(); it != s->ready.end() && looked < window; ++looked) {
+      Job *j = *it;
+      if (s->in_use + j->bytes <= s->budget) {
+        s->in_use += j->bytes;
+        s->peak = std::max(s->peak, s->in_use);
+        s->ready_bytes -= (size_t)j->req.nx * j->req.ny * j->req.nz * 16;
+        take.push_back(j);
+        it = s->ready.erase(it);
+      } else {
+        ++it;
+      }
+    }
+    if (!take.empty()) s->cv_prep.notify_all();
+  }
+  int n = 0;
+  for (Job *j : take) {
+    heat_desc d{};
+    d.nx = j->req.nx;
+    d.ny = j->req.ny;
+    d.nz = j->req.nz;
+    d.h = j->h;
+    d.dt = j->dt;
+    d.kappa = j->kappa.data();
+    d.u0 = j->u0.data();
+    d.precision = j->req.precision;
+    d.stream = s->stream;
+    int rc = heat_init(&j->ctx, &d);
+    if (rc == HEAT_OK) rc = heat_batch_add(s->batch, j->ctx, j->req.steps);
+    std::vector<double>().swap(j->kappa);
+    std::vector<double>().swap(j->u0);
+    j->admit_ms = now_ms(s);
+    if (rc != HEAT_OK) {
+      if (j->ctx) heat_destroy(j->ctx);
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->in_use -= j->bytes;
+      }
+      finish(s, j, rc, 0, 0);
+      delete j;
+      continue;
+    }
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->n_admitted += 1;
+      if (s->first_admit_ms < 0) s->first_admit_ms = j->admit_ms;
+      s->resident.push_back(j);
+    }
+    ++n;
+  }
+  return n;
+}
+
+void retire(heat_server *s) {
+  for (size_t q = 0; q < s->resident.size();) {
+    Job *j = s->resident[q];
+    long long left = 0;
+    heat_batch_pending(s->batch, j->ctx, &left);
+    if (left > 0) {
+      ++q;
+      continue;
+    }
+    double l2 = 0, cs = 0;
+    int rc = heat_norm(j->ctx, &l2, &cs);
+    if (rc == HEAT_OK && j->req.field_out) rc = heat_get_field(j->ctx, j->req.field_out);
+    heat_batch_remove(s->batch, j->ctx);
+    heat_destroy(j->ctx);
+    j->ctx = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->in_use -= j->bytes;
+    }
+    finish(s, j, rc, l2, cs);
+    delete j;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->resident.erase(s->resident.begin() + (long)q);
+  }
+}
+
+void worker_loop(heat_server *s) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_work.wait(lk, [&] { return s->stop || !s->ready.empty() || !s->resident.empty(); });
+      if (s->stop && s->resident.empty()) return;
+    }
+    admit(s);
+    bool any;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      any = !s->resident.empty();
+    }
+    if (any) {
+      const double t = now_ms(s);
+      long long taken = 0;
+      int rc = heat_batch_run(s->batch, s->tick_steps, &taken);
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->busy_ms += now_ms(s) - t;
+        if (rc != HEAT_OK) s->worker_status = rc;
+      }
+      retire(s);
+    } else {
+      // Nothing resident and nothing admitted: requests at the head of the
+      // queue need more than the whole budget and are rejected.
+      std::vector<Job *> reject;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        for (auto it = s->ready.begin(); it != s->ready.end();) {
+          if ((*it)->bytes > s->budget) {
+            s->ready_bytes -= (size_t)(*it)->req.nx * (*it)->req.ny * (*it)->req.nz * 16;
+            reject.push_back(*it);
+            it = s->ready.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      }
+      for (Job *j : reject) {
+        finish(s, j, HEAT_EBUDGET, 0, 0);
+        delete j;
+      }
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int heat_server_create(heat_server **out, size_t budget_bytes, int tick_steps, int prep_threads) {
+  if (!out || budget_bytes == 0 || tick_steps < 1 || prep_threads < 1) return HEAT_EINVAL;
+  *out = nullptr;
+  heat_server *s = new (std::nothrow) heat_server();
+  if (!s) return HEAT_ENOMEM;
+  s->budget = budget_bytes;
+  s->prep_cap = std::min<size_t>(budget_bytes, (size_t)16 << 30);
+  s->tick_steps = tick_steps;
+  s->t0 = Clock::now();
+  cudaGetDevice(&s->device);
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete s;
+    return HEAT_ECUDA;
+  }
+  int rc = heat_batch_create(&s->batch, s->stream, 0);
+  if (rc != HEAT_OK) {
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return rc;
+  }
+  for (int t = 0; t < prep_threads; ++t) s->preps.emplace_back(prep_loop, s);
+  s->worker = std::thread(worker_loop, s);
+  *out = s;
+  return HEAT_OK;
+}
+
+int heat_server_submit(heat_server *s, const heat_request *r, uint64_t *id_out) {
+  if (!s || !r) return HEAT_EINVAL;
+  if (r->nx < 3 || r->ny < 3 || r->nz < 3 || r->steps < 0 || r->cfg < 0 || r->cfg > 4 ||
+      (r->precision != HEAT_FP64 && r->precision != HEAT_FP32C))
+    return HEAT_EINVAL;
+  Job *j = new (std::nothrow) Job();
+  if (!j) return HEAT_ENOMEM;
+  j->req = *r;
+  j->bytes = request_bytes(*r);
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) {
+    delete j;
+    return HEAT_ESTATE;
+  }
+  j->id = s->next_id++;
+  j->submit_ms = now_ms(s);
+  s->n_submitted += 1;
+  s->submitted.push_back(j);
+  s->cv_prep.notify_one();
+  if (id_out) *id_out = j->id;
+  return HEAT_OK;
+}
+
+int heat_server_poll(heat_server *s, heat_result *out, int max, int *n_out) {
+  if (!s || (!out && max > 0) || max < 0) return HEAT_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  int n = std::min<int>(max, (int)s->done.size());
+  for (int i = 0; i < n; ++i) out[i] = s->done[i];
+  s->done.erase(s->done.begin(), s->done.begin() + n);
+  if (n_out) *n_out = n;
+  return s->worker_status;
+}
+
+int heat_server_wait_idle(heat_server *s) {
+  if (!s) return HEAT_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  s->cv_idle.wait(lk, [&] {
+    return (s->n_completed + s->n_rejected == s->n_submitted) || s->worker_status != HEAT_OK;
+  });
+  return s->worker_status;
+}
+
+int heat_server_stats(heat_server *s, heat_server_summary *st) {
+  if (!s || !st) return HEAT_EINVAL;
+  std::memset(st, 0, sizeof *st);
+  std::vector<double> lat;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    st->submitted = s->n_submitted;
+    st->admitted = s->n_admitted;
+    st->completed = s->n_completed;
+    st->rejected = s->n_rejected;
+    st->resident = (long long)s->resident.size();
+    st->queued = (long long)(s->submitted.size() + s->ready.size()) + s->preparing;
+    st->budget_bytes = s->budget;
+    st->bytes_in_use = s->in_use;
+    st->peak_bytes = s->peak;
+    st->busy_ms = s->busy_ms;
+    st->updates = s->updates_done;
+    const double span = s->last_done_ms - std::max(0.0, s->first_admit_ms);
+    st->glups = span > 0 ? s->updates_done / (span * 1e-3) / 1e9 : 0.0;
+    lat = s->latencies;
+  }
+  if (!lat.empty()) {
+    std::sort(lat.begin(), lat.end());
+    auto pct = [&](double p) {
+      size_t k = (size_t)std::min<double>((double)lat.size() - 1, p * (double)(lat.size() - 1) + 0.5);
+      return lat[k];
+    };
+    st->p50_ms = pct(0.50);
+    st->p99_ms = pct(0.99);
+    st->max_ms = lat.back();
+    double sum = 0;
+    for (double x : lat) sum += x;
+    st->mean_ms = sum / (double)lat.size();
+  }
+  long long kl = 0, gl = 0, bs = 0;
+  heat_batch_stats(s->batch, &kl, &gl, &bs);
+  st->kernel_launches = kl;
+  st->batch_steps = bs;
+  return HEAT_OK;
+}
+
+int heat_server_destroy(heat_server *s) {
+  if (!s) return HEAT_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    // Requests not yet on the GPU are dropped; resident ones finish.
+    for (Job *j : s->submitted) delete j;
+    for (Job *j : s->ready) delete j;
+    s->submitted.clear();
+    s->ready.clear();
+  }
+  s->cv_prep.notify_all();
+  s->cv_work.notify_all();
+  for (auto &t : s->preps) t.join();
+  if (s->worker.joinable()) s->worker.join();
+  heat_batch_destroy(s->batch);
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return HEAT_OK;
+}
+
+}  // extern "C"

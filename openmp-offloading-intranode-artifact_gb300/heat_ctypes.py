@@ -56,6 +56,28 @@ class HeatDesc(C.Structure):
 
 _dp = C.POINTER(C.c_double)
 
+
+class HeatRequest(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("steps", C.c_longlong),
+                ("precision", C.c_int), ("cfg", C.c_int), ("seed", C.c_uint64),
+                ("field_out", C.c_void_p)]
+
+
+class HeatResult(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int), ("l2", C.c_double), ("checksum", C.c_double),
+                ("submit_ms", C.c_double), ("admit_ms", C.c_double), ("done_ms", C.c_double),
+                ("updates", C.c_double)]
+
+
+class HeatServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("completed", C.c_longlong),
+                ("rejected", C.c_longlong), ("resident", C.c_longlong), ("queued", C.c_longlong),
+                ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("max_ms", C.c_double), ("glups", C.c_double), ("updates", C.c_double),
+                ("busy_ms", C.c_double), ("budget_bytes", C.c_size_t), ("bytes_in_use", C.c_size_t),
+                ("peak_bytes", C.c_size_t), ("batch_steps", C.c_longlong),
+                ("kernel_launches", C.c_longlong)]
+
 # Every symbol include/heat.h declares, with its ctypes signature.
 SIGNATURES = {
     "heat_init": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(HeatDesc)]),
@@ -83,6 +105,12 @@ SIGNATURES = {
     "heat_batch_destroy": (C.c_int, [C.c_void_p]),
     "heat_tune_batch": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.c_int]),
     "heat_tune_lookup": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.POINTER(C.c_int)]),
+    "heat_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t, C.c_int, C.c_int]),
+    "heat_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "heat_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "heat_server_wait_idle": (C.c_int, [C.c_void_p]),
+    "heat_server_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "heat_server_destroy": (C.c_int, [C.c_void_p]),
     "heat_inputs_reference": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, _dp, _dp]),
     "heat_inputs_config": (C.c_int, [C.c_int, C.c_uint64, C.c_int, C.c_int, C.c_int,
                                      C.c_void_p, C.c_void_p, _dp, _dp]),
@@ -278,3 +306,61 @@ def tune_lookup(precision: int, flags: int, nz: int) -> int:
     k = C.c_int()
     check(lib().heat_tune_lookup(precision, flags, nz, C.byref(k)), "heat_tune_lookup")
     return k.value
+
+
+class Server:
+    """heat_server: continuous-batching solves under an HBM budget."""
+
+    def __init__(self, budget_bytes: int, tick_steps: int = 64, prep_threads: int = 4):
+        self._s = C.c_void_p()
+        self._keep = {}
+        check(lib().heat_server_create(C.byref(self._s), budget_bytes, tick_steps, prep_threads),
+              "heat_server_create")
+
+    def submit(self, nx: int, ny: int, nz: int, steps: int, precision: int = HEAT_FP64,
+               cfg: int = 0, seed: int = 0, field_out: np.ndarray | None = None) -> int:
+        if field_out is not None:
+            assert field_out.shape == (nz, ny, nx) and field_out.dtype == np.float64
+            assert field_out.flags.c_contiguous
+        r = HeatRequest(nx, ny, nz, steps, precision, cfg, seed,
+                        None if field_out is None else field_out.ctypes.data)
+        rid = C.c_uint64()
+        check(lib().heat_server_submit(self._s, C.byref(r), C.byref(rid)), "heat_server_submit")
+        if field_out is not None:
+            self._keep[rid.value] = field_out
+        return rid.value
+
+    def poll(self, max_results: int = 1024) -> list[dict]:
+        buf = (HeatResult * max_results)()
+        n = C.c_int()
+        check(lib().heat_server_poll(self._s, buf, max_results, C.byref(n)), "heat_server_poll")
+        out = []
+        for r in buf[: n.value]:
+            out.append({k: getattr(r, k) for k, _ in HeatResult._fields_})
+            self._keep.pop(r.id, None)
+        return out
+
+    def wait_idle(self) -> None:
+        check(lib().heat_server_wait_idle(self._s), "heat_server_wait_idle")
+
+    def stats(self) -> dict:
+        st = HeatServerStats()
+        check(lib().heat_server_stats(self._s, C.byref(st)), "heat_server_stats")
+        return {k: getattr(st, k) for k, _ in HeatServerStats._fields_}
+
+    def close(self) -> None:
+        if self._s:
+            lib().heat_server_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
