@@ -61,6 +61,9 @@ extern "C" {
 /* Use only the hardware FP64 pipe in the default FP64 form (no integer
  * accumulation); for comparison runs.                                         */
 #define HEAT_HWFP64     0x4u
+/* HEAT_FP32C: one time step per launch.  By default pairs of steps run in
+ * one launch with TMA-staged plane tiles (bit-identical results).            */
+#define HEAT_NO_TEMPORAL 0x8u
 
 typedef struct heat_ctx heat_ctx;
 
@@ -73,7 +76,8 @@ typedef struct heat_desc {
   const double *u0;        /* host, nz*ny*nx, initial field (boundary kept)  */
   const double *rhs;       /* host, nz*ny*nx, per-step source; NULL = none   */
   int precision;           /* HEAT_FP64 | HEAT_FP32C                         */
-  unsigned flags;          /* HEAT_BITEXACT | HEAT_NAIVE | HEAT_HWFP64       */
+  unsigned flags;          /* HEAT_BITEXACT | HEAT_NAIVE | HEAT_HWFP64 |
+                              HEAT_NO_TEMPORAL                               */
   void *stream;            /* cudaStream_t to use, or NULL for an own stream */
 } heat_desc;
 

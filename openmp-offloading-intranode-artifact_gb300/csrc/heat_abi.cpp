@@ -17,7 +17,7 @@ thread_local char g_last_error[256] = "";
 
 // Warps (of 8 per block) of the hybrid FP64 kernel that run on the FP64 pipe;
 // the others run the integer-pipe evaluation.
-constexpr int kDefaultHwRows = 3;
+constexpr int kDefaultHwRows = 4;
 
 int cuda_fail(cudaError_t e, const char *what) {
   std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
@@ -39,12 +39,14 @@ bool geom_ok(int nx, int ny, int nz) {
   return true;
 }
 
-heat_geom make_geom(int nx, int ny, int nz) {
+// Row pitch: a multiple of 4 points (32-byte FP64 rows); FP32C fields use a
+// multiple of 8 so BF16 carry rows are multiples of 16 bytes for TMA.
+heat_geom make_geom(int nx, int ny, int nz, int align = 4) {
   heat_geom g;
   g.nx = nx;
   g.ny = ny;
   g.nz = nz;
-  g.pitch = (nx + 3) & ~3;
+  g.pitch = (nx + align - 1) / align * align;
   g.plane = (size_t)g.pitch * ny;
   g.elems = g.plane * nz;
   return g;
@@ -84,7 +86,7 @@ void free_ctx(heat_ctx *c) {
   void *ptrs[] = {c->u[0],   c->u[1],     c->rhs,      c->kappa,    c->ks[0],   c->ks[1],
                   c->ks[2],  c->c0,       c->cf[0],    c->cf[1],    c->cf[2],   c->kq,
                   c->v[0],   c->v[1],     c->carry[0], c->carry[1], c->fcf[0],  c->fcf[1],
-                  c->fcf[2], c->frhs,     c->partials};
+                  c->fcf[2], c->frhs,     c->partials, c->err};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -113,6 +115,19 @@ int launch_step(heat_ctx *c) {
   return HEAT_OK;
 }
 
+
+// HEAT_ETIMEOUT if a kernel of this context reported a bounded wait running
+// out (the flag is cleared once reported).  Synchronises the stream.
+int check_err(heat_ctx *c) {
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (flag) {
+    CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+    return HEAT_ETIMEOUT;
+  }
+  return HEAT_OK;
+}
 
 int widen_current(heat_ctx *c, double **out) {
   int rc = dalloc(out, c->g.elems);
@@ -155,7 +170,9 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
   TRY(dalloc(&kap, g.elems));
   TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
   c->n_partials = heat::kNormBlocks;
-  if (cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
+  TRY(dalloc(&c->err, 1));
+  if (cudaMemsetAsync(c->err, 0, sizeof(int), c->stream) != cudaSuccess ||
+      cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
       cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemset");
     goto done;
@@ -247,6 +264,11 @@ int init_fp32c(heat_ctx *c, const heat_desc *d) {
   for (int a = 0; a < 3; ++a) TRY(dalloc(&c->fcf[a], g.elems));
   TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
   c->n_partials = heat::kNormBlocks;
+  TRY(dalloc(&c->err, 1));
+  if (cudaMemsetAsync(c->err, 0, sizeof(int), c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+    goto done;
+  }
   TRY(dalloc(&tmp, g.elems));
   TRY(load_split(c, tmp, d->u0));
   if (cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream) != cudaSuccess) {
@@ -313,7 +335,7 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
 
   heat_ctx *c = new (std::nothrow) heat_ctx();
   if (!c) return HEAT_ENOMEM;
-  c->g = make_geom(d->nx, d->ny, d->nz);
+  c->g = make_geom(d->nx, d->ny, d->nz, d->precision == HEAT_FP32C ? 8 : 4);
   c->h = d->h;
   c->dt = d->dt;
   c->factor = d->dt / d->h / d->h / 2.0;  // as heat3D_variable_coeff.c:84
@@ -342,7 +364,20 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
 
 int heat_step(heat_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return HEAT_EINVAL;
-  for (int s = 0; s < nsteps; ++s) {
+  int s = 0;
+  if (c->precision == HEAT_FP32C && !c->frhs && !(c->flags & HEAT_NO_TEMPORAL) &&
+      heat::fp32c_tb2_ok(c->g)) {
+    // Two steps per launch; the result lands in the other buffer.
+    for (; s + 2 <= nsteps; s += 2) {
+      cudaError_t e = heat::launch_fp32c_tb2(c->v[c->cur ^ 1], c->carry[c->cur ^ 1], c->v[c->cur],
+                                             c->carry[c->cur], c->fcf, c->g, c->err, c->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "two-step kernel launch");
+      c->launches += 1;
+      c->cur ^= 1;
+      c->steps_done += 2;
+    }
+  }
+  for (; s < nsteps; ++s) {
     int rc = launch_step(c);
     if (rc != HEAT_OK) return rc;
   }
@@ -379,6 +414,7 @@ int heat_norm(heat_ctx *c, double *l2, double *checksum) {
   CK(cudaMemcpyAsync(r, c->partials + 2 * c->n_partials, sizeof r, cudaMemcpyDeviceToHost,
                      c->stream));
   CK(cudaStreamSynchronize(c->stream));
+  if (int rc = check_err(c)) return rc;
   if (checksum) *checksum = r[0];
   if (l2) *l2 = std::sqrt(r[1]);
   return HEAT_OK;
@@ -428,7 +464,7 @@ int heat_set_field(heat_ctx *c, const double *u_host) {
 int heat_sync(heat_ctx *c) {
   if (!c) return HEAT_EINVAL;
   CK(cudaStreamSynchronize(c->stream));
-  return HEAT_OK;
+  return check_err(c);
 }
 
 int heat_stats(heat_ctx *c, long long *steps_done, long long *kernel_launches) {

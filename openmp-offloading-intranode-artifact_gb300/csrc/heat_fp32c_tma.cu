@@ -1,0 +1,373 @@
+// FP32-compensated form, two time steps per launch (temporal blocking), with
+// plane tiles staged into shared memory by TMA.
+//
+// A block owns a (32 x 16) tile of output columns and walks a chunk of planes;
+// it has one thread per point of the tile plus a 1-point halo (34 x 18).
+// For every plane p the block's thread 0 issues TMA 3-D box loads
+// (cp.async.bulk.tensor) of the five input arrays -- v, carry, wx, wy, wz --
+// covering the tile plus a 2-point halo into one slot of a 4-deep shared
+// memory ring, completing on that slot's mbarrier; loads run two planes ahead
+// of use.  Each iteration k then
+//   1. computes step t+1 on plane k+1 over the tile plus a 1-point halo
+//      (34 x 18 points) from ring planes k, k+1, k+2 into a 3-plane ring of
+//      intermediate values, and
+//   2. computes step t+2 on plane k over the tile from intermediate planes
+//      k-1, k, k+1 and writes it to global memory.
+// Global traffic per two updates: the five input arrays read once (plus the
+// halo, mostly served by L2) and v, carry written once -- about half of two
+// single steps.  The per-point arithmetic is exactly the single-step column
+// walk's (walk_fp32c: same operations, same order, the intermediate carry
+// rounded to BF16 as the single step stores it), so two steps here are
+// bit-identical to two single steps.  Points on the grid boundary keep their
+// values at both levels.
+//
+// Every mbarrier wait is bounded: if a load does not complete within the
+// limit the block records the failure in *err, waits (bounded) for its other
+// loads in flight, and returns; the host reports HEAT_ETIMEOUT.
+
+#include <cuda.h>
+
+#include "heat_internal.h"
+#include "heat_walk.cuh"
+
+namespace heat {
+namespace {
+
+constexpr int OX = 32, OY = 16;          // output tile
+constexpr int BXF = 40, BXC = 48, BY = 20;  // TMA boxes (float arrays, BF16 carry)
+constexpr int L1X = OX + 2, L1Y = OY + 2;   // step-(t+1) region
+constexpr int NT = ((L1X * L1Y + 31) / 32) * 32;  // one thread per step-(t+1) point
+constexpr int R = 4;                     // ring depth (planes)
+
+constexpr int kPlaneF = BXF * BY;        // floats per float-array plane tile
+constexpr int kPlaneC = BXC * BY;        // BF16 per carry plane tile
+constexpr unsigned kSlotBytes = 4u * kPlaneF * 4u + 2u * kPlaneC;  // v, wx, wy, wz + carry
+constexpr unsigned kWaitLimit = 1u << 26;
+
+struct __align__(128) Slot {
+  float v[kPlaneF];
+  float wx[kPlaneF];
+  float wy[kPlaneF];
+  float wz[kPlaneF];
+  uint16_t c[kPlaneC];
+};
+
+struct Smem {
+  Slot ring[R];
+  float v1[3][NT];
+  unsigned long long bar[R];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long *b) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(unsigned long long *b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it)
+    if (mbar_try(b, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void tma_load3(void *dst, const CUtensorMap *map, int x, int y, int z,
+                                          unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+struct Maps {
+  CUtensorMap v, c, wx, wy, wz;
+};
+
+__global__ void __launch_bounds__(NT, 3)
+    k_fp32c_tb2(const __grid_constant__ Maps in, float *__restrict__ vn,
+                uint16_t *__restrict__ cn, int nx, int ny, int nz, int P, size_t S, int kchunk,
+                int *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int x0 = 1 + OX * blockIdx.x, y0 = 1 + OY * blockIdx.y;
+  const int kb = 1 + blockIdx.z * kchunk;
+  const int ke = min(kb + kchunk, nz - 1);
+  if (kb >= ke) return;
+  const int X0 = x0 - 5, X0c = x0 - 9, Y0 = y0 - 2;  // box origins (X0 % 4 == 0, X0c % 8 == 0)
+  const int pmin = max(kb - 2, 0), pmax = min(ke + 1, nz - 1);
+
+  if (tid == 0) {
+    for (int s = 0; s < R; ++s) mbar_init(&sm.bar[s]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  // Every thread keeps the same bookkeeping (which slots have a load in
+  // flight, and each slot's next completion parity); thread 0 issues the TMA
+  // and warp 0 alone spins on the mbarrier -- the block barrier after the
+  // wait hands the landed tile to the other warps.
+  unsigned pending = 0, phase = 0;
+  bool failed = false;
+  const bool waiter = tid < 32;
+  auto issue = [&](int p) {
+    if (p < pmin || p > pmax) return;
+    const int s = p % R;
+    pending |= 1u << s;
+    if (tid != 0) return;
+    Slot &sl = sm.ring[s];
+    unsigned long long *b = &sm.bar[s];
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect(b, kSlotBytes);
+    tma_load3(sl.v, &in.v, X0, Y0, p, b);
+    tma_load3(sl.wx, &in.wx, X0, Y0, p, b);
+    tma_load3(sl.wy, &in.wy, X0, Y0, p, b);
+    tma_load3(sl.wz, &in.wz, X0, Y0, p, b);
+    tma_load3(sl.c, &in.c, X0c, Y0, p, b);
+  };
+  auto wait_plane = [&](int p) {
+    if (p < pmin || p > pmax || failed) return;
+    const int s = p % R;
+    if (waiter && !mbar_wait(&sm.bar[s], (phase >> s) & 1u)) {
+      failed = true;
+      return;
+    }
+    phase ^= 1u << s;
+    pending &= ~(1u << s);
+  };
+
+  for (int p = kb - 2; p <= kb + 1; ++p) issue(p);
+
+  // This thread's step-(t+1) point (lx, ly) in the (34 x 18) region and its
+  // smem offsets; threads with 1 <= lx <= 32, 1 <= ly <= 16 also own an
+  // output point.  Like the single-step walk, each thread carries its own
+  // column along z in registers: the centre values of the input planes, the
+  // step-(t+1) values it computed, and the face weights it already loaded;
+  // only neighbours come from shared memory.
+  const bool l1_ok = tid < L1X * L1Y;
+  const int lx = tid % L1X, ly = tid / L1X;
+  const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+  const int o = (ly + 1) * BXF + (lx + 4);     // float box offset
+  const int oc = (ly + 1) * BXC + (lx + 8);    // carry box offset
+  const bool edge = gx <= 0 || gy <= 0 || gx >= nx - 1 || gy >= ny - 1;
+  const bool out_ok = l1_ok && lx >= 1 && lx <= OX && ly >= 1 && ly <= OY && gx < nx - 1 &&
+                      gy < ny - 1;
+
+  struct W {
+    float x, xm, y, ym, z;  // wx[c], wx[c-1], wy[c], wy[c-P], wz[c] at one plane
+  };
+  // Step t+1 on plane p at this thread's point from centre values vm, v0, vp
+  // (planes p-1, p, p+1) and wz at plane p-1; returns the new value and carry
+  // and the plane's weights.
+  auto level1 = [&](int p, float vm, float v0, float vp, float wzm, W &wp, float &t1,
+                    float &c1) {
+    const Slot &cur = sm.ring[p % R];
+    wp.x = cur.wx[o];
+    wp.xm = cur.wx[o - 1];
+    wp.y = cur.wy[o];
+    wp.ym = cur.wy[o - BXF];
+    wp.z = cur.wz[o];
+    const float cc0 = walk::bf2f(cur.c[oc]);
+    if (edge || p == 0 || p == nz - 1) {
+      t1 = v0;
+      c1 = cc0;
+      return;
+    }
+    float d = 0.0f;
+    d = fmaf(wp.x, cur.v[o + 1] - v0, d);
+    d = fmaf(wp.xm, cur.v[o - 1] - v0, d);
+    d = fmaf(wp.y, cur.v[o + BXF] - v0, d);
+    d = fmaf(wp.ym, cur.v[o - BXF] - v0, d);
+    d = fmaf(wp.z, vp - v0, d);
+    d = fmaf(wzm, vm - v0, d);
+    const float yk = __fsub_rn(d, cc0);
+    t1 = __fadd_rn(v0, yk);
+    c1 = walk::bf2f(walk::f2bf(__fsub_rn(__fsub_rn(t1, v0), yk)));
+  };
+
+  // Prologue: intermediate planes kb-1 and kb.  A failed wait stops the whole
+  // block (the decision is made block-wide).
+  wait_plane(kb - 2);
+  wait_plane(kb - 1);
+  wait_plane(kb);
+  wait_plane(kb + 1);
+  failed = __syncthreads_or(failed);
+  float vm = 0.f, v0 = 0.f, wzm = 0.f;    // level-1 window: v(p-1), v(p), wz(p-1)
+  float l1m = 0.f, l1c = 0.f, c1c = 0.f;  // own step-(t+1) values at k-1, k; carry at k
+  float wz2m = 0.f;                       // wz at plane k-1 (for step t+2 at k)
+  W wc{};                                 // weights at plane k (for step t+2 at k)
+  if (!failed && l1_ok) {
+    if (kb - 2 >= 0) {
+      vm = sm.ring[(kb - 2) % R].v[o];
+      wzm = sm.ring[(kb - 2) % R].wz[o];
+    }
+    v0 = sm.ring[(kb - 1) % R].v[o];
+    W wa;
+    float ta, ca;
+    float vp = sm.ring[kb % R].v[o];
+    level1(kb - 1, vm, v0, vp, wzm, wa, ta, ca);
+    sm.v1[(kb - 1) % 3][tid] = ta;
+    vm = v0;
+    v0 = vp;
+    wzm = wa.z;
+    W wb;
+    float tb, cb;
+    vp = sm.ring[(kb + 1) % R].v[o];
+    level1(kb, vm, v0, vp, wzm, wb, tb, cb);
+    sm.v1[kb % 3][tid] = tb;
+    vm = v0;
+    v0 = vp;
+    wzm = wb.z;
+    l1m = ta;
+    l1c = tb;
+    c1c = cb;
+    wz2m = wa.z;
+    wc = wb;
+  }
+  // The prologue's reads of planes kb-2 and kb-1 are done: their slots take
+  // planes kb+2 and kb+3.
+  __syncthreads();
+  if (!failed) {
+    issue(kb + 2);
+    issue(kb + 3);
+  }
+
+  size_t g = (size_t)kb * S + (size_t)gy * P + gx;
+  for (int k = kb; k < ke && !failed; ++k, g += S) {
+    wait_plane(k + 2);
+    // One barrier both publishes plane k+2 and retires iteration k-1: plane
+    // k's ring slot (read last by level 1 of plane k) and intermediate slot
+    // (k+1) % 3 are free after it.  Weights of planes k and k-1 live in
+    // registers, so only planes k+1 and k+2 stay resident.
+    failed = __syncthreads_or(failed);
+    if (failed) break;
+    issue(k + 4);
+    W wn{};
+    float l1p = 0.f, c1p = 0.f;
+    if (l1_ok) {
+      const float vp = sm.ring[(k + 2) % R].v[o];
+      level1(k + 1, vm, v0, vp, wzm, wn, l1p, c1p);
+      sm.v1[(k + 1) % 3][tid] = l1p;
+      vm = v0;
+      v0 = vp;
+      wzm = wn.z;
+    }
+    __syncthreads();
+    if (out_ok) {
+      const float *vk = sm.v1[k % 3];
+      float d = 0.0f;
+      d = fmaf(wc.x, vk[tid + 1] - l1c, d);
+      d = fmaf(wc.xm, vk[tid - 1] - l1c, d);
+      d = fmaf(wc.y, vk[tid + L1X] - l1c, d);
+      d = fmaf(wc.ym, vk[tid - L1X] - l1c, d);
+      d = fmaf(wc.z, l1p - l1c, d);
+      d = fmaf(wz2m, l1m - l1c, d);
+      const float yk = __fsub_rn(d, c1c);
+      const float t = __fadd_rn(l1c, yk);
+      const float cc = __fsub_rn(__fsub_rn(t, l1c), yk);
+      vn[g] = t;
+      cn[g] = walk::f2bf(cc);
+    }
+    l1m = l1c;
+    l1c = l1p;
+    c1c = c1p;
+    wz2m = wc.z;
+    wc = wn;
+  }
+  if (failed) {
+    if (tid == 0) atomicExch(err, 1);
+    // Let the block's own loads in flight land before its shared memory goes
+    // (each wait bounded).
+    if (waiter)
+      for (int s = 0; s < R; ++s)
+        if (pending & (1u << s)) mbar_wait(&sm.bar[s], (phase >> s) & 1u);
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encoder() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return (EncodeTiledFn) nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+bool encode(CUtensorMap *m, const void *base, bool bf16, const heat_geom &g) {
+  EncodeTiledFn fn = encoder();
+  if (!fn) return false;
+  const size_t es = bf16 ? 2 : 4;
+  cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
+  cuuint64_t strides[2] = {(cuuint64_t)g.pitch * es, (cuuint64_t)g.plane * es};
+  cuuint32_t box[3] = {(cuuint32_t)(bf16 ? BXC : BXF), (cuuint32_t)BY, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+            const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+size_t fp32c_tb2_smem() { return sizeof(Smem) + 128; }
+
+// Whether the two-step kernel can run this geometry: row and plane strides in
+// bytes must be multiples of 16 for TMA (pitch a multiple of 8 points).
+bool fp32c_tb2_ok(const heat_geom &g) {
+  return (g.pitch % 8) == 0 && g.nx >= 3 && encoder() != nullptr;
+}
+
+cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
+                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st) {
+  Maps m;
+  if (!encode(&m.v, v, false, g) || !encode(&m.c, cr, true, g) || !encode(&m.wx, w[0], false, g) ||
+      !encode(&m.wy, w[1], false, g) || !encode(&m.wz, w[2], false, g))
+    return cudaErrorInvalidValue;
+  static bool attr = [] {
+    return cudaFuncSetAttribute(k_fp32c_tb2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)fp32c_tb2_smem()) == cudaSuccess;
+  }();
+  if (!attr) return cudaErrorInvalidConfiguration;
+  const int bx = (g.nx - 2 + OX - 1) / OX, by = (g.ny - 2 + OY - 1) / OY;
+  const int interior = g.nz - 2;
+  long tiles = (long)bx * by;
+  long chunks = std::max(1L, std::min<long>(interior / 16, (4L * 456 + tiles - 1) / tiles));
+  const int kchunk = (int)((interior + chunks - 1) / chunks);
+  dim3 grid(bx, by, (interior + kchunk - 1) / kchunk);
+  k_fp32c_tb2<<<grid, NT, fp32c_tb2_smem(), st>>>(m, v_new, c_new, g.nx, g.ny, g.nz, g.pitch,
+                                                  g.plane, kchunk, err);
+  return cudaGetLastError();
+}
+
+}  // namespace heat

@@ -45,6 +45,9 @@ struct heat_ctx {
   float *fcf[3];            // FP32 face weights
   float *frhs;              // FP32 source (NULL when none)
 
+  // Device flag a kernel sets when a bounded wait ran out (HEAT_ETIMEOUT).
+  int *err;
+
   // Norm scratch: per-block partial sums, then the final pair.
   double *partials;
   int n_partials;
@@ -98,6 +101,11 @@ cudaError_t launch_widen(double *u, const float *v, const uint16_t *cr, size_t t
 cudaError_t launch_f32_weights(float *const w[3], const double *kappa, const heat_geom &g,
                                double factor, cudaStream_t st);
 cudaError_t launch_to_f32(float *o, const double *a, size_t total, cudaStream_t st);
+
+// heat_fp32c_tma.cu: two steps per launch (temporal blocking, TMA staging).
+bool fp32c_tb2_ok(const heat_geom &g);
+cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
+                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st);
 
 // heat_reduce.cu
 cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,

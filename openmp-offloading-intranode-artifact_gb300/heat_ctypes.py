@@ -32,6 +32,7 @@ HEAT_FP32C = 1
 HEAT_BITEXACT = 0x1
 HEAT_NAIVE = 0x2
 HEAT_HWFP64 = 0x4
+HEAT_NO_TEMPORAL = 0x8
 
 HEAT_BATCH_NO_GRAPHS = 0x1
 HEAT_BATCH_PERSISTENT = 0x2
