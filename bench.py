@@ -45,7 +45,8 @@ CFG = 1
 METRIC = "GLUP/s (FP64 plain heat stencil, 512^3, 1000 steps per solve)"
 UNIT = "GLUP/s"
 BYTES_PER_UPDATE = 24.0   # u read 8 + u write 8 + kappa read 8 (compulsory, FP64)
-FP32C_BYTES_PER_UPDATE = 24.0  # v 4+4, carry 2+2, three FP32 face weights 12
+FP32C_BYTES_PER_UPDATE = 24.0  # one step: v 4+4, carry 2+2, three FP32 face weights 12
+FP32C_BYTES_PER_UPDATE_TB2 = 12.0  # two steps per launch: the same 24 B per two updates
 H100_1CUDA_N512 = 38.97   # reference 1-cuda, H100, N=512 (CUDA/summary.csv:2)
 
 
@@ -327,9 +328,11 @@ def our_arm(a):
                     "ms_per_step": round(e2e_s * 1e3, 3)},
             "fp32c": {"value": round(fp32c_value, 3), "unit": UNIT,
                       "vs_fp64": round(fp32c_value / (value / world), 3),
-                      "bytes_per_update": FP32C_BYTES_PER_UPDATE,
-                      "hbm_frac": round(fp32c_value * FP32C_BYTES_PER_UPDATE / hbm_peak, 4),
-                      "note": "FP32 u + BF16 Kahan carry, FP32 face weights; same workload, "
+                      "bytes_per_update": FP32C_BYTES_PER_UPDATE_TB2,
+                      "hbm_frac": round(fp32c_value * FP32C_BYTES_PER_UPDATE_TB2 / hbm_peak, 4),
+                      "hbm_frac_single_step_bytes": round(fp32c_value * FP32C_BYTES_PER_UPDATE / hbm_peak, 4),
+                      "note": "FP32 u + BF16 Kahan carry, FP32 face weights, two steps per launch "
+                              "(TMA-staged temporal blocking); same workload, "
                               f"{ts} steps, CUDA events; errors: profiles/fp32c_precision.md"},
             "gpu_launches": int(l1 - l0),
             "clocks": clk.summary(),

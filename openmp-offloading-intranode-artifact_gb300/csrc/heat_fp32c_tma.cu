@@ -42,7 +42,8 @@ constexpr int R = 4;                     // ring depth (planes)
 constexpr int kPlaneF = BXF * BY;        // floats per float-array plane tile
 constexpr int kPlaneC = BXC * BY;        // BF16 per carry plane tile
 constexpr unsigned kSlotBytes = 4u * kPlaneF * 4u + 2u * kPlaneC;  // v, wx, wy, wz + carry
-constexpr unsigned kWaitLimit = 1u << 26;
+constexpr unsigned kSuspendNs = 2000;     // try_wait suspend-time hint
+constexpr unsigned kWaitLimit = 1u << 22; // bounded wait: attempts before giving up
 
 struct __align__(128) Slot {
   float v[kPlaneF];
@@ -72,14 +73,17 @@ __device__ __forceinline__ void mbar_expect(unsigned long long *b, unsigned byte
                : "memory");
 }
 
+// try_wait with a suspend-time hint: the waiting thread sleeps in the
+// instruction (up to ~the hint) instead of spinning and taking issue slots
+// from the warps that compute.
 __device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity) {
   unsigned ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity)
+      : "r"(smem_u32(b)), "r"(parity), "r"(kSuspendNs)
       : "memory");
   return ok != 0;
 }

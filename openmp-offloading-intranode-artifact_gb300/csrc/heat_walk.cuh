@@ -228,13 +228,35 @@ __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *_
                                         size_t c, int kb, int ke) {
   double ud = u[c - S], uc = u[c];
   double wd = cz[c - S];
+  // The plane's loads are issued one iteration ahead: next to the integer
+  // warps of the hybrid launch these warps are few, and would otherwise wait
+  // on memory instead of keeping the FP64 pipe busy.
+  double nu = u[c + S], nwu = cz[c], nc0 = c0[c], nr = RHS ? rhs[c] : 0.0;
+  double nxe = cx[c], nxw = cx[c - 1], nyn = cy[c], nys = cy[c - P];
+  double ne = u[c + 1], nw = u[c - 1], nn = u[c + P], ns = u[c - P];
   for (int k = kb; k < ke; ++k, c += S) {
-    const double uu = u[c + S], wu = cz[c];
-    double acc = RHS ? fma(c0[c], uc, rhs[c]) : c0[c] * uc;
-    acc = fma(cx[c], u[c + 1], acc);
-    acc = fma(cx[c - 1], u[c - 1], acc);
-    acc = fma(cy[c], u[c + P], acc);
-    acc = fma(cy[c - P], u[c - P], acc);
+    const double uu = nu, wu = nwu, w0 = nc0, r = nr, xe = nxe, xw = nxw, yn = nyn, ys = nys;
+    const double ue = ne, uw = nw, un_ = nn, us = ns;
+    if (k + 1 < ke) {
+      const size_t q = c + S;
+      nu = u[q + S];
+      nwu = cz[q];
+      nc0 = c0[q];
+      if (RHS) nr = rhs[q];
+      nxe = cx[q];
+      nxw = cx[q - 1];
+      nyn = cy[q];
+      nys = cy[q - P];
+      ne = u[q + 1];
+      nw = u[q - 1];
+      nn = u[q + P];
+      ns = u[q - P];
+    }
+    double acc = RHS ? fma(w0, uc, r) : w0 * uc;
+    acc = fma(xe, ue, acc);
+    acc = fma(xw, uw, acc);
+    acc = fma(yn, un_, acc);
+    acc = fma(ys, us, acc);
     acc = fma(wu, uu, acc);
     acc = fma(wd, ud, acc);
     un[c] = acc;
