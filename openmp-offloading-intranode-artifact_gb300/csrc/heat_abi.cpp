@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 
 #include "heat_diag.h"
@@ -52,10 +53,44 @@ heat_geom make_geom(int nx, int ny, int nz, int align = 4) {
   return g;
 }
 
+// Device memory of contexts comes from one stream-ordered pool per device, so
+// creating and destroying contexts (the server does so continuously) never
+// calls cudaMalloc/cudaFree, whose device-wide synchronisation would stall
+// every other stream.  Freed blocks stay cached up to a quarter of the device
+// memory for reuse.
+cudaMemPool_t device_pool(int dev) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    uint64_t keep = total_b / 4;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaGetLastError();
+    pools[dev] = pool;
+  }
+  return pools[dev];
+}
+
 template <class T>
-int dalloc(T **p, size_t count) {
+int dalloc(T **p, size_t count, cudaStream_t st) {
   *p = nullptr;
-  cudaError_t e = cudaMalloc((void **)p, count * sizeof(T));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaMemPool_t pool = device_pool(dev);
+  cudaError_t e = pool ? cudaMallocFromPoolAsync((void **)p, count * sizeof(T), pool, st)
+                       : cudaMalloc((void **)p, count * sizeof(T));
   if (e != cudaSuccess) {
     *p = nullptr;
     cudaGetLastError();
@@ -88,7 +123,7 @@ void free_ctx(heat_ctx *c) {
                   c->v[0],   c->v[1],     c->carry[0], c->carry[1], c->fcf[0],  c->fcf[1],
                   c->fcf[2], c->frhs,     c->partials, c->err};
   for (void *p : ptrs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, c->stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -130,7 +165,7 @@ int check_err(heat_ctx *c) {
 }
 
 int widen_current(heat_ctx *c, double **out) {
-  int rc = dalloc(out, c->g.elems);
+  int rc = dalloc(out, c->g.elems, c->stream);
   if (rc != HEAT_OK) return rc;
   cudaError_t e = heat::launch_widen(*out, c->v[c->cur], c->carry[c->cur], c->g.elems, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "widen");
@@ -165,12 +200,12 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
     rc = (x);                     \
     if (rc != HEAT_OK) goto done; \
   } while (0)
-  TRY(dalloc(&c->u[0], g.elems));
-  TRY(dalloc(&c->u[1], g.elems));
-  TRY(dalloc(&kap, g.elems));
-  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
+  TRY(dalloc(&c->u[0], g.elems, c->stream));
+  TRY(dalloc(&c->u[1], g.elems, c->stream));
+  TRY(dalloc(&kap, g.elems, c->stream));
+  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2, c->stream));
   c->n_partials = heat::kNormBlocks;
-  TRY(dalloc(&c->err, 1));
+  TRY(dalloc(&c->err, 1, c->stream));
   if (cudaMemsetAsync(c->err, 0, sizeof(int), c->stream) != cudaSuccess ||
       cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
       cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
@@ -187,7 +222,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
     goto done;
   }
   if (d->rhs) {
-    TRY(dalloc(&c->rhs, g.elems));
+    TRY(dalloc(&c->rhs, g.elems, c->stream));
     if (cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaMemset");
       goto done;
@@ -198,7 +233,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
     c->kappa = kap;
     kap = nullptr;
   } else if (c->flags & HEAT_BITEXACT) {
-    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->ks[a], g.elems));
+    for (int a = 0; a < 3; ++a) TRY(dalloc(&c->ks[a], g.elems, c->stream));
     {
       cudaError_t e = heat::launch_face_sums(c->ks, kap, g, c->stream);
       if (e != cudaSuccess) { rc = cuda_fail(e, "face sums"); goto done; }
@@ -215,7 +250,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
     if (use_int) {
       // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
       // the FP64-pipe kernel when the fixed-point range check fails.
-      TRY(dalloc(&c->kq, g.elems));
+      TRY(dalloc(&c->kq, g.elems, c->stream));
       int bad = 0;
       int *d_bad = reinterpret_cast<int *>(c->partials);
       cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
@@ -226,14 +261,14 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
       if (e != cudaSuccess) { rc = cuda_fail(e, "fixed-point setup"); goto done; }
       c->launches += 1;
       if (bad) {
-        cudaFree(c->kq);
+        cudaFreeAsync(c->kq, c->stream);
         c->kq = nullptr;
         use_int = false;
       }
     }
     if (!use_int || c->hw_rows > 0) {
-      TRY(dalloc(&c->c0, g.elems));
-      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems));
+      TRY(dalloc(&c->c0, g.elems, c->stream));
+      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems, c->stream));
       cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);
       if (e != cudaSuccess) { rc = cuda_fail(e, "coefficients"); goto done; }
       c->launches += 1;
@@ -242,7 +277,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
   if (cudaStreamSynchronize(c->stream) != cudaSuccess)
     rc = cuda_fail(cudaGetLastError(), "heat_init sync");
 done:
-  if (kap) cudaFree(kap);
+  if (kap) cudaFreeAsync(kap, c->stream);
   return rc;
 #undef TRY
 }
@@ -258,18 +293,18 @@ int init_fp32c(heat_ctx *c, const heat_desc *d) {
     if (rc != HEAT_OK) goto done; \
   } while (0)
   for (int b = 0; b < 2; ++b) {
-    TRY(dalloc(&c->v[b], g.elems));
-    TRY(dalloc(&c->carry[b], g.elems));
+    TRY(dalloc(&c->v[b], g.elems, c->stream));
+    TRY(dalloc(&c->carry[b], g.elems, c->stream));
   }
-  for (int a = 0; a < 3; ++a) TRY(dalloc(&c->fcf[a], g.elems));
-  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2));
+  for (int a = 0; a < 3; ++a) TRY(dalloc(&c->fcf[a], g.elems, c->stream));
+  TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2, c->stream));
   c->n_partials = heat::kNormBlocks;
-  TRY(dalloc(&c->err, 1));
+  TRY(dalloc(&c->err, 1, c->stream));
   if (cudaMemsetAsync(c->err, 0, sizeof(int), c->stream) != cudaSuccess) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemset");
     goto done;
   }
-  TRY(dalloc(&tmp, g.elems));
+  TRY(dalloc(&tmp, g.elems, c->stream));
   TRY(load_split(c, tmp, d->u0));
   if (cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream) != cudaSuccess) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemset");
@@ -280,7 +315,7 @@ int init_fp32c(heat_ctx *c, const heat_desc *d) {
   if (e != cudaSuccess) { rc = cuda_fail(e, "FP32 weights"); goto done; }
   c->launches += 1;
   if (d->rhs) {
-    TRY(dalloc(&c->frhs, g.elems));
+    TRY(dalloc(&c->frhs, g.elems, c->stream));
     if (cudaMemsetAsync(tmp, 0, g.elems * sizeof(double), c->stream) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaMemset");
       goto done;
@@ -293,7 +328,7 @@ int init_fp32c(heat_ctx *c, const heat_desc *d) {
   if (cudaStreamSynchronize(c->stream) != cudaSuccess)
     rc = cuda_fail(cudaGetLastError(), "heat_init sync");
 done:
-  if (tmp) cudaFree(tmp);
+  if (tmp) cudaFreeAsync(tmp, c->stream);
   return rc;
 #undef TRY
 }
@@ -432,7 +467,7 @@ int heat_get_field(heat_ctx *c, double *u_host) {
   int rc = widen_current(c, &tmp);
   if (rc == HEAT_OK) rc = download(u_host, tmp, c->g, c->stream);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  if (tmp) cudaFree(tmp);
+  if (tmp) cudaFreeAsync(tmp, c->stream);
   if (rc != HEAT_OK) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "heat_get_field");
   return HEAT_OK;
@@ -451,11 +486,11 @@ int heat_set_field(heat_ctx *c, const double *u_host) {
     return HEAT_OK;
   }
   double *tmp = nullptr;
-  int rc = dalloc(&tmp, c->g.elems);
+  int rc = dalloc(&tmp, c->g.elems, c->stream);
   if (rc != HEAT_OK) return rc;
   rc = load_split(c, tmp, u_host);
   cudaError_t e = cudaStreamSynchronize(c->stream);
-  cudaFree(tmp);
+  cudaFreeAsync(tmp, c->stream);
   if (rc != HEAT_OK) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "heat_set_field");
   return HEAT_OK;
@@ -525,7 +560,7 @@ int heat_diag_field_diff(heat_ctx *a, heat_ctx *b, double *max_abs, double *rel_
     if (b->precision == HEAT_FP64) fb = b->u[b->cur];
     else if ((rc = widen_current(b, &tb)) == HEAT_OK) fb = tb;
   }
-  if (rc == HEAT_OK) rc = dalloc(&part, 3 * (size_t)nb + 3);
+  if (rc == HEAT_OK) rc = dalloc(&part, 3 * (size_t)nb + 3, (cudaStream_t)0);
   if (rc == HEAT_OK) {
     e = cudaDeviceSynchronize();
     if (e == cudaSuccess) e = heat::launch_diff_f64(fa, fb, a->g, part, nb, (cudaStream_t)0);
@@ -533,9 +568,9 @@ int heat_diag_field_diff(heat_ctx *a, heat_ctx *b, double *max_abs, double *rel_
       e = cudaMemcpy(r, part + 3 * nb, sizeof r, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) rc = cuda_fail(e, "field diff");
   }
-  if (ta) cudaFree(ta);
-  if (tb) cudaFree(tb);
-  if (part) cudaFree(part);
+  if (ta) cudaFreeAsync(ta, a->stream);
+  if (tb) cudaFreeAsync(tb, b->stream);
+  if (part) cudaFreeAsync(part, (cudaStream_t)0);
   if (rc != HEAT_OK) return rc;
   if (max_abs) *max_abs = r[2];
   if (rel_l2) *rel_l2 = r[1] > 0 ? std::sqrt(r[0] / r[1]) : std::sqrt(r[0]);

@@ -39,10 +39,22 @@ struct heat_batch {
   std::vector<Entry> entries;
   std::vector<int> active;  // entry indices in table order
 
-  heat::BatchGrid *d_grids = nullptr;
-  size_t cap_grids = 0;
-  heat::BatchTile *d_tiles = nullptr;
-  size_t cap_tiles = 0;
+  // Two device copies of the tables: a rebuild fills the one not used by the
+  // launches still in flight (each copy's event marks its last use).
+  heat::BatchGrid *g_buf[2] = {nullptr, nullptr};
+  size_t g_cap[2] = {0, 0};
+  heat::BatchTile *t_buf[2] = {nullptr, nullptr};
+  size_t t_cap[2] = {0, 0};
+  cudaEvent_t table_ev[2] = {nullptr, nullptr};
+  bool table_used[2] = {false, false};
+  // Table uploads run on their own stream (a pageable upload first waits for
+  // everything queued on its stream; this one has nothing queued), and the
+  // batch stream waits on copy_ev before the next launch.
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_ev = nullptr;
+  int tb = 0;                          // table copy in use
+  heat::BatchGrid *d_grids = nullptr;  // == g_buf[tb]
+  heat::BatchTile *d_tiles = nullptr;  // == t_buf[tb]
   int ntiles = 0;
   // Tiles are grouped by form: form f owns [tile_begin[f], tile_begin[f] + tile_count[f]).
   int tile_begin[heat::kNumKinds] = {};
@@ -101,8 +113,16 @@ void release(heat_batch *b) {
     if (b->join_ev[f]) cudaEventDestroy(b->join_ev[f]);
   }
   if (b->fork_ev) cudaEventDestroy(b->fork_ev);
-  if (b->d_grids) cudaFree(b->d_grids);
-  if (b->d_tiles) cudaFree(b->d_tiles);
+  if (b->copy_stream) {
+    cudaStreamSynchronize(b->copy_stream);
+    cudaStreamDestroy(b->copy_stream);
+  }
+  if (b->copy_ev) cudaEventDestroy(b->copy_ev);
+  for (int i = 0; i < 2; ++i) {
+    if (b->g_buf[i]) cudaFree(b->g_buf[i]);
+    if (b->t_buf[i]) cudaFree(b->t_buf[i]);
+    if (b->table_ev[i]) cudaEventDestroy(b->table_ev[i]);
+  }
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -218,18 +238,30 @@ int rebuild(heat_batch *b) {
     long long nb = std::max(1LL, (long long)(share * full + 0.5));
     b->form_blocks[f] = (int)std::min<long long>(nb, b->tile_count[f]);
   }
-  int rc = grow(&b->d_grids, &b->cap_grids, std::max<size_t>(1, grids.size()));
-  if (rc == HEAT_OK) rc = grow(&b->d_tiles, &b->cap_tiles, std::max<size_t>(1, tiles.size()));
-  if (rc != HEAT_OK) return rc;
-  if (!grids.empty() &&
-      (cudaMemcpyAsync(b->d_grids, grids.data(), grids.size() * sizeof(heat::BatchGrid),
-                       cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
-       cudaMemcpyAsync(b->d_tiles, tiles.data(), tiles.size() * sizeof(heat::BatchTile),
-                       cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
-       cudaStreamSynchronize(b->stream) != cudaSuccess)) {
+  // Fill the table copy the in-flight launches are not using (waiting, if
+  // need be, for the launches that used it last).
+  const int nb = b->tb ^ 1;
+  if (b->table_used[nb] && cudaEventSynchronize(b->table_ev[nb]) != cudaSuccess) {
     cudaGetLastError();
     return HEAT_ECUDA;
   }
+  int rc = grow(&b->g_buf[nb], &b->g_cap[nb], std::max<size_t>(1, grids.size()));
+  if (rc == HEAT_OK) rc = grow(&b->t_buf[nb], &b->t_cap[nb], std::max<size_t>(1, tiles.size()));
+  if (rc != HEAT_OK) return rc;
+  // Pageable sources: the copies are staged before the calls return.
+  if (!grids.empty() &&
+      (cudaMemcpyAsync(b->g_buf[nb], grids.data(), grids.size() * sizeof(heat::BatchGrid),
+                       cudaMemcpyHostToDevice, b->copy_stream) != cudaSuccess ||
+       cudaMemcpyAsync(b->t_buf[nb], tiles.data(), tiles.size() * sizeof(heat::BatchTile),
+                       cudaMemcpyHostToDevice, b->copy_stream) != cudaSuccess ||
+       cudaEventRecord(b->copy_ev, b->copy_stream) != cudaSuccess ||
+       cudaStreamWaitEvent(b->stream, b->copy_ev, 0) != cudaSuccess)) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
+  b->tb = nb;
+  b->d_grids = b->g_buf[nb];
+  b->d_tiles = b->t_buf[nb];
   b->ntiles = (int)tiles.size();
   b->since_build = 0;
   b->dirty = false;
@@ -275,11 +307,17 @@ cudaError_t enqueue_steps(heat_batch *b, int p, int n) {
   return err;
 }
 
+void mark_table_use(heat_batch *b) {
+  cudaEventRecord(b->table_ev[b->tb], b->stream);
+  b->table_used[b->tb] = true;
+}
+
 int launch_plain(heat_batch *b, int n) {
   if (enqueue_steps(b, (int)(b->since_build & 1), n) != cudaSuccess) {
     cudaGetLastError();
     return HEAT_ECUDA;
   }
+  mark_table_use(b);
   b->launches += (long long)n * b->nforms;
   advance(b, n);
   return HEAT_OK;
@@ -331,7 +369,11 @@ int heat_batch_create(heat_batch **out, void *stream, unsigned flags) {
   for (int f = 0; f < heat::kNumKinds; ++f) b->blocks_per_sm[f] = heat::batch_blocks_per_sm(f);
   b->persistent = (flags & HEAT_BATCH_PERSISTENT) != 0;
   b->concurrent = (flags & HEAT_BATCH_SERIAL_FORMS) == 0;
-  bool ok = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) == cudaSuccess;
+  bool ok = cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->table_ev[0], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->table_ev[1], cudaEventDisableTiming) == cudaSuccess &&
+            cudaEventCreateWithFlags(&b->copy_ev, cudaEventDisableTiming) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
   for (int f = 0; f < heat::kNumKinds && ok; ++f)
     ok = cudaStreamCreateWithFlags(&b->side[f], cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&b->join_ev[f], cudaEventDisableTiming) == cudaSuccess;
@@ -378,7 +420,8 @@ int heat_batch_remove(heat_batch *b, heat_ctx *c) {
   if (!b || !c) return HEAT_EINVAL;
   for (size_t e = 0; e < b->entries.size(); ++e)
     if (b->entries[e].ctx == c) {
-      if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+      // A context with steps left may be in launches still running.
+      if (b->entries[e].remaining > 0 && cudaStreamSynchronize(b->stream) != cudaSuccess) {
         cudaGetLastError();
         return HEAT_ECUDA;
       }
@@ -399,7 +442,14 @@ int heat_batch_pending(heat_batch *b, heat_ctx *c, long long *steps_left) {
   return HEAT_EINVAL;
 }
 
-int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken) {
+}  // extern "C"
+
+namespace heat {
+
+// heat_batch_run without the final synchronisation: launches are queued on
+// the batch stream and the host bookkeeping (steps, current buffers) is
+// already advanced when it returns.
+int batch_run(heat_batch *b, long long max_steps, long long *steps_taken, bool sync) {
   if (!b) return HEAT_EINVAL;
   long long done = 0;
   int rc = HEAT_OK;
@@ -449,6 +499,7 @@ int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken) {
           }
           b->graph_launches += 1;
           b->launches += (long long)b->graph_steps * b->nforms;
+          mark_table_use(b);
           advance(b, b->graph_steps);
           done += b->graph_steps;
         }
@@ -465,12 +516,22 @@ int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken) {
       if (b->entries[e].remaining <= 0) b->dirty = true;
     if (max_steps >= 0 && done >= max_steps) break;
   }
-  if (cudaStreamSynchronize(b->stream) != cudaSuccess) {
+  if (sync && cudaStreamSynchronize(b->stream) != cudaSuccess) {
     cudaGetLastError();
     if (rc == HEAT_OK) rc = HEAT_ECUDA;
   }
   if (steps_taken) *steps_taken = done;
   return rc;
+}
+
+cudaStream_t batch_stream(heat_batch *b) { return b->stream; }
+
+}  // namespace heat
+
+extern "C" {
+
+int heat_batch_run(heat_batch *b, long long max_steps, long long *steps_taken) {
+  return heat::batch_run(b, max_steps, steps_taken, true);
 }
 
 int heat_batch_stats(heat_batch *b, long long *kernel_launches, long long *graph_launches,

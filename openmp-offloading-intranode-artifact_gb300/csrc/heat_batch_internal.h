@@ -53,4 +53,9 @@ int batch_form(const heat_ctx *c);
 // its size class, else a default.
 int tuned_kchunk(int form, int nz);
 
+// heat_batch_run with the final stream synchronisation optional (sync=false:
+// the launches are queued and the bookkeeping advanced on return).
+int batch_run(heat_batch *b, long long max_steps, long long *steps_taken, bool sync);
+cudaStream_t batch_stream(heat_batch *b);
+
 }  // namespace heat

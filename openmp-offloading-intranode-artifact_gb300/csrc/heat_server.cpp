@@ -9,14 +9,20 @@
 //            few behind it may be admitted first if they fit), create their
 //            contexts (fields stay device-resident until they finish) and add
 //            them to the batch with their step counts;
-//   advance: heat_batch_run for at most `tick_steps` batch steps -- every
-//            resident solve advances together, whatever its size and form;
-//   retire:  solves with no steps left report their norm (and field, if asked),
-//            release their memory and budget, and become results.
+//   advance: queue at most `tick_steps` batch steps -- every resident solve
+//            advances together, whatever its size and form -- and record a
+//            tick event; the worker does not wait for the tick;
+//   retire:  solves whose last step ran in a tick that has completed report
+//            their norm (and field, if asked), release their memory and
+//            budget, and become results.
 //
-// so requests arriving while others are on the GPU join at the next tick as
-// memory frees up, and their work overlaps on the device.  Latency of a
-// request = completion time - submission time.
+// Admission and retirement of one tick overlap with the GPU running the
+// previous one (at most two ticks are queued), so requests arriving while
+// others are on the GPU join at the next tick as memory frees up, and their
+// work overlaps on the device.  Each request's context has its own stream;
+// contexts allocate from the library's stream-ordered pool, so neither
+// admission nor retirement synchronises the device.  Latency of a request =
+// completion time - submission time.
 
 #include <algorithm>
 #include <atomic>
@@ -29,7 +35,7 @@
 #include <thread>
 #include <vector>
 
-#include "heat_internal.h"
+#include "heat_batch_internal.h"
 
 namespace {
 
@@ -44,6 +50,8 @@ struct Job {
   double h = 0, dt = 0;
   int status = HEAT_OK;
   heat_ctx *ctx = nullptr;
+  bool finished = false;          // all steps queued
+  cudaEvent_t finish_ev = nullptr;  // tick event after its last step (null: none ran)
 };
 
 // Device bytes a request holds while resident (fields, coefficient planes,
@@ -82,6 +90,8 @@ struct heat_server {
   heat_batch *batch = nullptr;
   cudaStream_t stream = nullptr;
   int device = 0;
+  std::vector<cudaEvent_t> ev_free;   // recycled tick events
+  std::deque<cudaEvent_t> ev_live;    // tick events of queued ticks, oldest first
   std::vector<std::thread> preps;
   std::thread worker;
   int worker_status = HEAT_OK;
@@ -192,7 +202,7 @@ int admit(heat_server *s) {
     d.kappa = j->kappa.data();
     d.u0 = j->u0.data();
     d.precision = j->req.precision;
-    d.stream = s->stream;
+    d.stream = nullptr;  // own stream: the context's work never waits on the batch
     int rc = heat_init(&j->ctx, &d);
     if (rc == HEAT_OK) rc = heat_batch_add(s->batch, j->ctx, j->req.steps);
     std::vector<double>().swap(j->kappa);
@@ -219,14 +229,21 @@ int admit(heat_server *s) {
   return n;
 }
 
-void retire(heat_server *s) {
-  for (size_t q = 0; q < s->resident.size();) {
-    Job *j = s->resident[q];
-    long long left = 0;
-    heat_batch_pending(s->batch, j->ctx, &left);
-    if (left > 0) {
-      ++q;
-      continue;
+// Retire finished solves whose last tick has completed (all of them if
+// `block`, waiting as needed).
+void retire(heat_server *s, bool block) {
+  std::vector<Job *> res;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    res = s->resident;
+  }
+  for (Job *j : res) {
+    if (!j->finished) continue;
+    if (j->finish_ev) {
+      if (!block && cudaEventQuery(j->finish_ev) == cudaErrorNotReady) continue;
+      cudaGetLastError();
+      // The norm (on the context's stream) follows the tick's kernels.
+      cudaStreamWaitEvent(j->ctx->stream, j->finish_ev, 0);
     }
     double l2 = 0, cs = 0;
     int rc = heat_norm(j->ctx, &l2, &cs);
@@ -237,11 +254,35 @@ void retire(heat_server *s) {
     {
       std::lock_guard<std::mutex> lk(s->mu);
       s->in_use -= j->bytes;
+      s->resident.erase(std::find(s->resident.begin(), s->resident.end(), j));
     }
     finish(s, j, rc, l2, cs);
     delete j;
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->resident.erase(s->resident.begin() + (long)q);
+  }
+}
+
+cudaEvent_t take_event(heat_server *s) {
+  cudaEvent_t e = nullptr;
+  if (!s->ev_free.empty()) {
+    e = s->ev_free.back();
+    s->ev_free.pop_back();
+  } else if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    e = nullptr;
+  }
+  return e;
+}
+
+// Return tick events no job refers to any more and whose ticks completed.
+void recycle_events(heat_server *s) {
+  while (s->ev_live.size() > 1) {
+    cudaEvent_t e = s->ev_live.front();
+    bool used = false;
+    for (Job *j : s->resident) used |= (j->finish_ev == e);
+    if (used || cudaEventQuery(e) == cudaErrorNotReady) break;
+    cudaGetLastError();
+    s->ev_live.pop_front();
+    s->ev_free.push_back(e);
   }
 }
 
@@ -251,39 +292,66 @@ void worker_loop(heat_server *s) {
     {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_work.wait(lk, [&] { return s->stop || !s->ready.empty() || !s->resident.empty(); });
-      if (s->stop && s->resident.empty()) return;
+      if (s->stop && s->resident.empty()) break;
     }
     admit(s);
-    bool any;
+    retire(s, false);
+    std::vector<Job *> res;
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      any = !s->resident.empty();
+      res = s->resident;
     }
-    if (any) {
+    bool active = false;
+    for (Job *j : res) {
+      long long left = 0;
+      heat_batch_pending(s->batch, j->ctx, &left);
+      if (left > 0) active = true;
+      else if (!j->finished) j->finished = true;  // nothing to run (0 steps)
+    }
+    if (active) {
       const double t = now_ms(s);
       long long taken = 0;
-      int rc = heat_batch_run(s->batch, s->tick_steps, &taken);
+      int rc = heat::batch_run(s->batch, s->tick_steps, &taken, false);
+      cudaEvent_t ev = take_event(s);
+      if (ev) {
+        cudaEventRecord(ev, s->stream);
+        s->ev_live.push_back(ev);
+      }
+      for (Job *j : res) {
+        if (j->finished) continue;
+        long long left = 0;
+        heat_batch_pending(s->batch, j->ctx, &left);
+        if (left == 0) {
+          j->finished = true;
+          j->finish_ev = ev;
+        }
+      }
+      // At most two ticks queued: wait for the one before this.
+      if (s->ev_live.size() >= 2) cudaEventSynchronize(s->ev_live[s->ev_live.size() - 2]);
       {
         std::lock_guard<std::mutex> lk(s->mu);
         s->busy_ms += now_ms(s) - t;
         if (rc != HEAT_OK) s->worker_status = rc;
       }
-      retire(s);
+      recycle_events(s);
     } else {
-      // Nothing resident and nothing admitted: requests at the head of the
-      // queue need more than the whole budget and are rejected.
+      // Nothing left to run: retire what finished (waiting for its tick), and
+      // reject requests that can never fit the budget.
+      retire(s, true);
+      recycle_events(s);
       std::vector<Job *> reject;
       {
         std::lock_guard<std::mutex> lk(s->mu);
-        for (auto it = s->ready.begin(); it != s->ready.end();) {
-          if ((*it)->bytes > s->budget) {
-            s->ready_bytes -= (size_t)(*it)->req.nx * (*it)->req.ny * (*it)->req.nz * 16;
-            reject.push_back(*it);
-            it = s->ready.erase(it);
-          } else {
-            ++it;
+        if (s->resident.empty())
+          for (auto it = s->ready.begin(); it != s->ready.end();) {
+            if ((*it)->bytes > s->budget) {
+              s->ready_bytes -= (size_t)(*it)->req.nx * (*it)->req.ny * (*it)->req.nz * 16;
+              reject.push_back(*it);
+              it = s->ready.erase(it);
+            } else {
+              ++it;
+            }
           }
-        }
       }
       for (Job *j : reject) {
         finish(s, j, HEAT_EBUDGET, 0, 0);
@@ -291,6 +359,11 @@ void worker_loop(heat_server *s) {
       }
     }
   }
+  cudaStreamSynchronize(s->stream);
+  for (cudaEvent_t e : s->ev_live) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->ev_free) cudaEventDestroy(e);
+  s->ev_live.clear();
+  s->ev_free.clear();
 }
 
 }  // namespace
