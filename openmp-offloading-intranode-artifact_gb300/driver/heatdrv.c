@@ -18,7 +18,13 @@
  * scripts parse it unchanged, and adds GLUP/s, L2 norm and checksum.  The
  * timer brackets the time loop and the final device synchronisation, as
  * 1-cuda.cu:231-257 does.  WRITE_TXT=0/false/no suppresses the %.17g k-j-i
- * dump (u_gb300_1gpu.txt), as the reference's should_write_txt().
+ * dump, as the reference's should_write_txt().
+ *
+ * The dump is named after the binary the driver is invoked as, so a link
+ * named like a reference binary takes its place in the reference's run and
+ * verify scripts: 1-omp writes u_openmp_1gpu.txt (1-openmp.c:228), 1-cuda
+ * writes u_cuda_1gpu.txt (1-cuda.cu:278), any other name u_gb300_1gpu.txt.
+ * HEAT_DUMP=<file> overrides the name.
  */
 #include <stdint.h>
 #include <stdio.h>
@@ -40,6 +46,16 @@ static int should_write_txt(void) {
   if (!e) return 1;
   if (!strcmp(e, "0") || !strcasecmp(e, "false") || !strcasecmp(e, "no")) return 0;
   return 1;
+}
+
+static const char *dump_name(const char *argv0) {
+  const char *e = getenv("HEAT_DUMP");
+  if (e && *e) return e;
+  const char *base = strrchr(argv0, '/');
+  base = base ? base + 1 : argv0;
+  if (!strcmp(base, "1-omp")) return "u_openmp_1gpu.txt";
+  if (!strcmp(base, "1-cuda")) return "u_cuda_1gpu.txt";
+  return "u_gb300_1gpu.txt";
 }
 
 static void die(const char *what, int rc) {
@@ -142,11 +158,12 @@ int main(int argc, char **argv) {
   if (should_write_txt()) {
     rc = heat_get_field(ctx, u0);
     if (rc != HEAT_OK) die("heat_get_field", rc);
-    FILE *f = fopen("u_gb300_1gpu.txt", "w");
+    const char *dump = dump_name(argv[0]);
+    FILE *f = fopen(dump, "w");
     if (!f) { perror("fopen"); return 1; }
     for (size_t q = 0; q < total; ++q) fprintf(f, "%.17g\n", u0[q]);
-    fclose(f);
-    printf("Solution written to %s\n", "u_gb300_1gpu.txt");
+    if (fclose(f) != 0) { perror("fclose"); return 1; }
+    printf("Solution written to %s\n", dump);
   }
   heat_destroy(ctx);
   free(kappa); free(u0); free(rhs);
