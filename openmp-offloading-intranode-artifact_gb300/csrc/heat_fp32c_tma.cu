@@ -28,6 +28,7 @@
 #include <cuda.h>
 
 #include "heat_internal.h"
+#include "heat_tma.cuh"
 #include "heat_walk.cuh"
 
 namespace heat {
@@ -42,8 +43,6 @@ constexpr int R = 4;                     // ring depth (planes)
 constexpr int kPlaneF = BXF * BY;        // floats per float-array plane tile
 constexpr int kPlaneC = BXC * BY;        // BF16 per carry plane tile
 constexpr unsigned kSlotBytes = 4u * kPlaneF * 4u + 2u * kPlaneC;  // v, wx, wy, wz + carry
-constexpr unsigned kSuspendNs = 2000;     // try_wait suspend-time hint
-constexpr unsigned kWaitLimit = 1u << 22; // bounded wait: attempts before giving up
 
 struct __align__(128) Slot {
   float v[kPlaneF];
@@ -59,48 +58,14 @@ struct Smem {
   unsigned long long bar[R];
 };
 
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long *b) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(b)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect(unsigned long long *b, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
-               "r"(bytes)
-               : "memory");
-}
-
-// try_wait with a suspend-time hint: the waiting thread sleeps in the
-// instruction (up to ~the hint) instead of spinning and taking issue slots
-// from the warps that compute.
-__device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity) {
-  unsigned ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(smem_u32(b)), "r"(parity), "r"(kSuspendNs)
-      : "memory");
-  return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it)
-    if (mbar_try(b, parity)) return true;
-  return false;
-}
+using tma::mbar_expect;
+using tma::mbar_init;
+using tma::mbar_wait;
+using tma::smem_u32;
 
 __device__ __forceinline__ void tma_load3(void *dst, const CUtensorMap *map, int x, int y, int z,
                                           unsigned long long *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
-      : "memory");
+  tma::load3(dst, map, x, y, z, bar);
 }
 
 struct Maps {
@@ -123,7 +88,7 @@ __global__ void __launch_bounds__(NT, 3)
 
   if (tid == 0) {
     for (int s = 0; s < R; ++s) mbar_init(&sm.bar[s]);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tma::mbar_init_fence();
   }
   __syncthreads();
 
@@ -141,7 +106,7 @@ __global__ void __launch_bounds__(NT, 3)
     if (tid != 0) return;
     Slot &sl = sm.ring[s];
     unsigned long long *b = &sm.bar[s];
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tma::fence_proxy_async();
     mbar_expect(b, kSlotBytes);
     tma_load3(sl.v, &in.v, X0, Y0, p, b);
     tma_load3(sl.wx, &in.wx, X0, Y0, p, b);
@@ -308,38 +273,10 @@ __global__ void __launch_bounds__(NT, 3)
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encoder() {
-  static EncodeTiledFn fn = [] {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess) {
-      cudaGetLastError();
-      return (EncodeTiledFn) nullptr;
-    }
-    return reinterpret_cast<EncodeTiledFn>(p);
-  }();
-  return fn;
-}
-
 bool encode(CUtensorMap *m, const void *base, bool bf16, const heat_geom &g) {
-  EncodeTiledFn fn = encoder();
-  if (!fn) return false;
-  const size_t es = bf16 ? 2 : 4;
-  cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
-  cuuint64_t strides[2] = {(cuuint64_t)g.pitch * es, (cuuint64_t)g.plane * es};
-  cuuint32_t box[3] = {(cuuint32_t)(bf16 ? BXC : BXF), (cuuint32_t)BY, 1};
-  cuuint32_t estr[3] = {1, 1, 1};
-  return fn(m, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-            const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  return tma::encode_field(m, base,
+                           bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                           bf16 ? 2 : 4, g, bf16 ? BXC : BXF, BY);
 }
 
 }  // namespace
@@ -349,7 +286,7 @@ size_t fp32c_tb2_smem() { return sizeof(Smem) + 128; }
 // Whether the two-step kernel can run this geometry: row and plane strides in
 // bytes must be multiples of 16 for TMA (pitch a multiple of 8 points).
 bool fp32c_tb2_ok(const heat_geom &g) {
-  return (g.pitch % 8) == 0 && g.nx >= 3 && encoder() != nullptr;
+  return (g.pitch % 8) == 0 && g.nx >= 3 && tma::encoder() != nullptr;
 }
 
 cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,

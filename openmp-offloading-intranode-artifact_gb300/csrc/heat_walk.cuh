@@ -157,101 +157,167 @@ __device__ __noinline__ double slow_point(double uc, double ue, double uw, doubl
 
 constexpr u64 kSign = 0x8000000000000000ull;
 
-// The integer-pipe walk over one (i, j) column, planes [kb, ke).
+// Raw bits of a point's stencil, for the per-point FP64 path that inputs
+// with infinities or NaNs take.
+struct Raw7 {
+  u64 c, e, w, n, s, u, d;
+};
+
+// One point of the integer-pipe evaluation from its decoded stencil and the
+// fixed-point weights K of the point and its six neighbours; br is the bits
+// of the source term (RHS only).  raw() yields the stencil's raw bits, read
+// only on the per-point FP64 path.
+template <bool RHS, class RawFn>
+__device__ __forceinline__ double int_point(const Dec &dc, const Dec &du, const Dec &dd,
+                                            const Dec &de, const Dec &dw, const Dec &dn,
+                                            const Dec &ds, u64 Kc, u64 Ku, u64 Kd, u64 Ke,
+                                            u64 Kw, u64 Kn, u64 Ks, u64 br, RawFn raw) {
+  int E = max(max(max(dc.e, du.e), max(dd.e, de.e)), max(max(dw.e, dn.e), ds.e));
+  Dec dr;
+  if (RHS) {
+    dr = decode(br);
+    E = max(E, dr.e);
+  }
+  if (E < 2047) {
+    const i64 Ac = align(dc, E);
+    const u64 We = Kc + Ke, Ww = Kc + Kw, Wn = Kc + Kn, Ws = Kc + Ks, Wu = Kc + Ku, Wd = Kc + Kd;
+    // Each product is taken of D + 2^63 (D = A_f - A_C, |D| < 2^63) so it is
+    // unsigned; the offsets sum to (sum_f W_f) / 2, removed up front.  (+ 2^63
+    // is the same as ^ 2^63 modulo 2^64, and folds into the subtraction.)
+    u64 acc = (u64)Ac - ((We + Ww + Wn + Ws + Wu + Wd) >> 1);
+    mac_hi(acc, (u64)(align(de, E) - Ac) + kSign, We);
+    mac_hi(acc, (u64)(align(dw, E) - Ac) + kSign, Ww);
+    mac_hi(acc, (u64)(align(dn, E) - Ac) + kSign, Wn);
+    mac_hi(acc, (u64)(align(ds, E) - Ac) + kSign, Ws);
+    mac_hi(acc, (u64)(align(du, E) - Ac) + kSign, Wu);
+    mac_hi(acc, (u64)(align(dd, E) - Ac) + kSign, Wd);
+    if (RHS) acc += (u64)align(dr, E);
+    return encode((i64)acc, E);
+  }
+  const Raw7 r = raw();
+  return slow_point(__longlong_as_double(r.c), __longlong_as_double(r.e),
+                    __longlong_as_double(r.w), __longlong_as_double(r.n),
+                    __longlong_as_double(r.s), __longlong_as_double(r.u),
+                    __longlong_as_double(r.d), RHS ? __longlong_as_double(br) : 0.0, Kc, Ke, Kw,
+                    Kn, Ks, Ku, Kd);
+}
+
+// Column state of the integer-pipe walk: one (i, j) column, advanced one
+// plane per step(); the next plane's loads are issued one step ahead.
 template <bool RHS>
-__device__ __forceinline__ void walk_int(double *__restrict__ un, const u64 *__restrict__ ub,
-                                         const double *__restrict__ rhs,
-                                         const u64 *__restrict__ K, int P, size_t S,
-                                         size_t c, int kb, int ke) {
-  u64 bd = ub[c - S], bc = ub[c];
-  Dec dd = decode(bd), dc = decode(bc);
-  u64 Kd = K[c - S], Kc = K[c];
-  // Loads of the next plane are issued one iteration ahead.
-  u64 nu = ub[c + S], ne = ub[c + 1], nw = ub[c - 1], nn = ub[c + P], ns = ub[c - P];
-  u64 mu = K[c + S], me = K[c + 1], mw = K[c - 1], mn = K[c + P], ms = K[c - P];
-  for (int k = kb; k < ke; ++k, c += S) {
+struct IntCol {
+  size_t c;
+  u64 bd, bc, Kd, Kc;
+  Dec dd, dc;
+  u64 nu, ne, nw, nn, ns, mu, me, mw, mn, ms;
+
+  __device__ __forceinline__ void fetch(const u64 *__restrict__ ub, const u64 *__restrict__ K,
+                                        int P, size_t S, size_t q) {
+    nu = ub[q + S]; ne = ub[q + 1]; nw = ub[q - 1]; nn = ub[q + P]; ns = ub[q - P];
+    mu = K[q + S]; me = K[q + 1]; mw = K[q - 1]; mn = K[q + P]; ms = K[q - P];
+  }
+
+  __device__ __forceinline__ void start(const u64 *__restrict__ ub, const u64 *__restrict__ K,
+                                        int P, size_t S, size_t c_) {
+    c = c_;
+    bd = ub[c - S];
+    bc = ub[c];
+    dd = decode(bd);
+    dc = decode(bc);
+    Kd = K[c - S];
+    Kc = K[c];
+    fetch(ub, K, P, S, c);
+  }
+
+  // Writes the new value of plane c and moves to the next plane; `more`
+  // says whether a next plane follows (its loads are issued now).
+  __device__ __forceinline__ void step(double *__restrict__ un, const u64 *__restrict__ ub,
+                                       const double *__restrict__ rhs,
+                                       const u64 *__restrict__ K, int P, size_t S, bool more) {
     const u64 bu = nu, be = ne, bw = nw, bn = nn, bs = ns;
     const u64 Ku = mu, Ke = me, Kw = mw, Kn = mn, Ks = ms;
-    if (k + 1 < ke) {
-      const size_t q = c + S;
-      nu = ub[q + S]; ne = ub[q + 1]; nw = ub[q - 1]; nn = ub[q + P]; ns = ub[q - P];
-      mu = K[q + S]; me = K[q + 1]; mw = K[q - 1]; mn = K[q + P]; ms = K[q - P];
-    }
+    if (more) fetch(ub, K, P, S, c + S);
     const Dec du = decode(bu), de = decode(be), dw = decode(bw), dn = decode(bn), ds = decode(bs);
-    int E = max(max(max(dc.e, du.e), max(dd.e, de.e)), max(max(dw.e, dn.e), ds.e));
-    Dec dr;
-    u64 br = 0;
-    if (RHS) {
-      br = __double_as_longlong(rhs[c]);
-      dr = decode(br);
-      E = max(E, dr.e);
-    }
-    double out;
-    if (E < 2047) {
-      const i64 Ac = align(dc, E);
-      const u64 We = Kc + Ke, Ww = Kc + Kw, Wn = Kc + Kn, Ws = Kc + Ks, Wu = Kc + Ku, Wd = Kc + Kd;
-      // Each product is taken of D + 2^63 (D = A_f - A_C, |D| < 2^63) so it is
-      // unsigned; the offsets sum to (sum_f W_f) / 2, removed up front.
-      u64 acc = (u64)Ac - ((We + Ww + Wn + Ws + Wu + Wd) >> 1);
-      mac_hi(acc, (u64)(align(de, E) - Ac) ^ kSign, We);
-      mac_hi(acc, (u64)(align(dw, E) - Ac) ^ kSign, Ww);
-      mac_hi(acc, (u64)(align(dn, E) - Ac) ^ kSign, Wn);
-      mac_hi(acc, (u64)(align(ds, E) - Ac) ^ kSign, Ws);
-      mac_hi(acc, (u64)(align(du, E) - Ac) ^ kSign, Wu);
-      mac_hi(acc, (u64)(align(dd, E) - Ac) ^ kSign, Wd);
-      if (RHS) acc += (u64)align(dr, E);
-      out = encode((i64)acc, E);
-    } else {
-      out = slow_point(__longlong_as_double(bc), __longlong_as_double(be), __longlong_as_double(bw),
-                       __longlong_as_double(bn), __longlong_as_double(bs),
-                       __longlong_as_double(bu), __longlong_as_double(bd),
-                       RHS ? __longlong_as_double(br) : 0.0, Kc, Ke, Kw, Kn, Ks, Ku, Kd);
-    }
-    un[c] = out;
+    const u64 br = RHS ? (u64)__double_as_longlong(rhs[c]) : 0ull;
+    const u64 bcc = bc, bdd = bd;
+    un[c] = int_point<RHS>(dc, du, dd, de, dw, dn, ds, Kc, Ku, Kd, Ke, Kw, Kn, Ks, br,
+                                [=] { return Raw7{bcc, be, bw, bn, bs, bu, bdd}; });
     bd = bc;
     bc = bu;
     dd = dc;
     dc = du;
     Kd = Kc;
     Kc = Ku;
+    c += S;
   }
+};
+
+// The integer-pipe walk over one (i, j) column, planes [kb, ke).
+template <bool RHS>
+__device__ __forceinline__ void walk_int(double *__restrict__ un, const u64 *__restrict__ ub,
+                                         const double *__restrict__ rhs,
+                                         const u64 *__restrict__ K, int P, size_t S,
+                                         size_t c, int kb, int ke) {
+  IntCol<RHS> col;
+  col.start(ub, K, P, S, c);
+  for (int k = kb; k < ke; ++k) col.step(un, ub, rhs, K, P, S, k + 1 < ke);
 }
 
-// The FP64-pipe walk (precomputed double weights, 7 FMA per point).
+// Column state of the FP64-pipe walk (precomputed double weights, 7 FMA per
+// point).  The plane's loads are issued one step ahead: next to the integer
+// warps of the hybrid launch these warps are few, and would otherwise wait
+// on memory instead of keeping the FP64 pipe busy.
 template <bool RHS>
-__device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *__restrict__ u,
+struct HwCol {
+  size_t c;
+  double ud, uc, wd;
+  double nu, nwu, nc0, nr, nxe, nxw, nyn, nys, ne, nw, nn, ns;
+
+  __device__ __forceinline__ void fetch(const double *__restrict__ u,
                                         const double *__restrict__ rhs,
                                         const double *__restrict__ c0,
                                         const double *__restrict__ cx,
                                         const double *__restrict__ cy,
                                         const double *__restrict__ cz, int P, size_t S,
-                                        size_t c, int kb, int ke) {
-  double ud = u[c - S], uc = u[c];
-  double wd = cz[c - S];
-  // The plane's loads are issued one iteration ahead: next to the integer
-  // warps of the hybrid launch these warps are few, and would otherwise wait
-  // on memory instead of keeping the FP64 pipe busy.
-  double nu = u[c + S], nwu = cz[c], nc0 = c0[c], nr = RHS ? rhs[c] : 0.0;
-  double nxe = cx[c], nxw = cx[c - 1], nyn = cy[c], nys = cy[c - P];
-  double ne = u[c + 1], nw = u[c - 1], nn = u[c + P], ns = u[c - P];
-  for (int k = kb; k < ke; ++k, c += S) {
+                                        size_t q) {
+    nu = u[q + S];
+    nwu = cz[q];
+    nc0 = c0[q];
+    nr = RHS ? rhs[q] : 0.0;
+    nxe = cx[q];
+    nxw = cx[q - 1];
+    nyn = cy[q];
+    nys = cy[q - P];
+    ne = u[q + 1];
+    nw = u[q - 1];
+    nn = u[q + P];
+    ns = u[q - P];
+  }
+
+  __device__ __forceinline__ void start(const double *__restrict__ u,
+                                        const double *__restrict__ rhs,
+                                        const double *__restrict__ c0,
+                                        const double *__restrict__ cx,
+                                        const double *__restrict__ cy,
+                                        const double *__restrict__ cz, int P, size_t S,
+                                        size_t c_) {
+    c = c_;
+    ud = u[c - S];
+    uc = u[c];
+    wd = cz[c - S];
+    fetch(u, rhs, c0, cx, cy, cz, P, S, c);
+  }
+
+  __device__ __forceinline__ void step(double *__restrict__ un, const double *__restrict__ u,
+                                       const double *__restrict__ rhs,
+                                       const double *__restrict__ c0,
+                                       const double *__restrict__ cx,
+                                       const double *__restrict__ cy,
+                                       const double *__restrict__ cz, int P, size_t S,
+                                       bool more) {
     const double uu = nu, wu = nwu, w0 = nc0, r = nr, xe = nxe, xw = nxw, yn = nyn, ys = nys;
     const double ue = ne, uw = nw, un_ = nn, us = ns;
-    if (k + 1 < ke) {
-      const size_t q = c + S;
-      nu = u[q + S];
-      nwu = cz[q];
-      nc0 = c0[q];
-      if (RHS) nr = rhs[q];
-      nxe = cx[q];
-      nxw = cx[q - 1];
-      nyn = cy[q];
-      nys = cy[q - P];
-      ne = u[q + 1];
-      nw = u[q - 1];
-      nn = u[q + P];
-      ns = u[q - P];
-    }
+    if (more) fetch(u, rhs, c0, cx, cy, cz, P, S, c + S);
     double acc = RHS ? fma(w0, uc, r) : w0 * uc;
     acc = fma(xe, ue, acc);
     acc = fma(xw, uw, acc);
@@ -263,7 +329,22 @@ __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *_
     ud = uc;
     uc = uu;
     wd = wu;
+    c += S;
   }
+};
+
+// The FP64-pipe walk over one (i, j) column, planes [kb, ke).
+template <bool RHS>
+__device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *__restrict__ u,
+                                        const double *__restrict__ rhs,
+                                        const double *__restrict__ c0,
+                                        const double *__restrict__ cx,
+                                        const double *__restrict__ cy,
+                                        const double *__restrict__ cz, int P, size_t S,
+                                        size_t c, int kb, int ke) {
+  HwCol<RHS> col;
+  col.start(u, rhs, c0, cx, cy, cz, P, S, c);
+  for (int k = kb; k < ke; ++k) col.step(un, u, rhs, c0, cx, cy, cz, P, S, k + 1 < ke);
 }
 
 // ---- FP32-compensated form ----

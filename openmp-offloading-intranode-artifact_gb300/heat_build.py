@@ -59,7 +59,7 @@ def _run(cmd: list[str]) -> None:
 def build(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     OBJ.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list((ROOT / "include").glob("*.h"))
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
     jobs = []
     for src in sorted(CSRC.glob("*.cu")):
         obj = OBJ / (src.name + ".o")
