@@ -128,28 +128,34 @@ void free_ctx(heat_ctx *c) {
   delete c;
 }
 
-int launch_step(heat_ctx *c) {
+// One step of context c from buffer `cur` into buffer cur ^ 1 on stream st,
+// with the kernel its form selects; the context's bookkeeping is untouched.
+cudaError_t enqueue_one(heat_ctx *c, int cur, cudaStream_t st) {
   const heat_geom &g = c->g;
-  double *uo = c->u[c->cur], *un = c->u[c->cur ^ 1];
-  cudaError_t e;
+  double *uo = c->u[cur], *un = c->u[cur ^ 1];
   if (c->precision == HEAT_FP32C)
-    e = heat::launch_fp32c(c->v[c->cur ^ 1], c->carry[c->cur ^ 1], c->v[c->cur],
-                           c->carry[c->cur], c->fcf, c->frhs, g, c->stream);
-  else if (c->flags & HEAT_NAIVE)
-    e = heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, c->stream);
-  else if (c->flags & HEAT_BITEXACT)
-    e = heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, c->stream);
-  else if (c->kq)
-    e = heat::launch_fast_mix(un, uo, c->rhs, c->kq, c->c0, c->cf, g, c->hw_rows, c->stream);
-  else
-    e = heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, c->stream, true);
+    return heat::launch_fp32c(c->v[cur ^ 1], c->carry[cur ^ 1], c->v[cur], c->carry[cur], c->fcf,
+                              c->frhs, g, st);
+  if (c->flags & HEAT_NAIVE) return heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, st);
+  if (c->flags & HEAT_BITEXACT)
+    return heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, st);
+  if (c->kq) return heat::launch_fast_mix(un, uo, c->rhs, c->kq, c->c0, c->cf, g, c->hw_rows, st);
+  return heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, st, true);
+}
+
+bool two_step_form(const heat_ctx *c) {
+  return c->precision == HEAT_FP32C && !c->frhs && !(c->flags & HEAT_NO_TEMPORAL) &&
+         heat::fp32c_tb2_ok(c->g);
+}
+
+int launch_step(heat_ctx *c) {
+  cudaError_t e = enqueue_one(c, c->cur, c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
   c->launches += 1;
   c->cur ^= 1;
   c->steps_done += 1;
   return HEAT_OK;
 }
-
 
 // HEAT_ETIMEOUT if a kernel of this context reported a bounded wait running
 // out (the flag is cleared once reported).  Synchronises the stream.
@@ -335,6 +341,34 @@ done:
 
 }  // namespace
 
+namespace heat {
+
+cudaError_t enqueue_ctx_steps(heat_ctx *c, int cur, long long n, cudaStream_t st,
+                              long long *launches) {
+  long long s = 0;
+  cudaError_t e = cudaSuccess;
+  if (two_step_form(c))
+    for (; s + 2 <= n && e == cudaSuccess; s += 2) {
+      // two steps per launch: the result lands in the other buffer
+      e = launch_fp32c_tb2(c->v[cur ^ 1], c->carry[cur ^ 1], c->v[cur], c->carry[cur], c->fcf, c->g,
+                           c->err, st);
+      cur ^= 1;
+      if (launches) ++*launches;
+    }
+  for (; s < n && e == cudaSuccess; ++s) {
+    e = enqueue_one(c, cur, st);
+    cur ^= 1;
+    if (launches) ++*launches;
+  }
+  return e;
+}
+
+int ctx_flips(const heat_ctx *c, long long n) {
+  return (int)((two_step_form(c) ? n / 2 + n % 2 : n) & 1);
+}
+
+}  // namespace heat
+
 extern "C" {
 
 const char *heat_strerror(int status) {
@@ -400,8 +434,7 @@ int heat_init(heat_ctx **out, const heat_desc *d) {
 int heat_step(heat_ctx *c, int nsteps) {
   if (!c || nsteps < 0) return HEAT_EINVAL;
   int s = 0;
-  if (c->precision == HEAT_FP32C && !c->frhs && !(c->flags & HEAT_NO_TEMPORAL) &&
-      heat::fp32c_tb2_ok(c->g)) {
+  if (two_step_form(c)) {
     // Two steps per launch; the result lands in the other buffer.
     for (; s + 2 <= nsteps; s += 2) {
       cudaError_t e = heat::launch_fp32c_tb2(c->v[c->cur ^ 1], c->carry[c->cur ^ 1], c->v[c->cur],

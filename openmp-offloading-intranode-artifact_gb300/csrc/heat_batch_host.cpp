@@ -10,11 +10,21 @@
 // source term) present together run on their own streams, forked from and
 // joined to the batch stream, unless HEAT_BATCH_SERIAL_FORMS.
 //
-// Bookkeeping: every active context advances one step per launch; the device
-// table records each grid's current buffer at build time and each launch gets
-// the parity of the steps taken since, so a graph of an even number of steps
-// can be replayed any number of times.  The table is rebuilt (and the graph
-// re-captured) only when the set of active contexts changes.
+// Grids large enough to fill the GPU alone (HEAT_BATCH_SOLO_POINTS interior
+// points, default 2,000,000) are stepped with their single-grid kernels
+// instead -- the FP64 hybrid launch, and two FP32C steps per launch -- on a
+// stream of their own beside the table kernels; the tile table carries the
+// small grids, which one launch per grid would leave the GPU mostly idle for.
+// On configuration 3 the table alone measured 106 GLUP/s, the grids one at a
+// time with their single-grid kernels 126.
+//
+// Bookkeeping: every active context advances one step per batch step; the
+// device table records each grid's current buffer at build time and each
+// launch gets the parity of the steps taken since.  A captured graph records
+// every grid's current buffer, and is replayed only while they match (a run
+// of an even number of steps returns table grids to the same buffers, and
+// two-step launches swap once per two steps).  The table is rebuilt (and the
+// graph re-captured) when the set of active contexts changes.
 
 #include <algorithm>
 #include <cstdio>
@@ -35,9 +45,14 @@ struct heat_batch {
     heat_ctx *ctx;
     long long remaining;
     long long base_steps;  // ctx->steps_done when the table was built
+    bool solo;             // stepped with its single-grid kernels
   };
   std::vector<Entry> entries;
-  std::vector<int> active;  // entry indices in table order
+  std::vector<int> active;  // entry indices in table order, then solo entries
+  std::vector<int> solo;    // the active entries stepped alone
+  long long solo_points = 2000000;
+  cudaStream_t solo_stream = nullptr;
+  cudaEvent_t solo_join = nullptr;
 
   // Two device copies of the tables: a rebuild fills the one not used by the
   // launches still in flight (each copy's event marks its last use).
@@ -69,7 +84,8 @@ struct heat_batch {
   long long since_build = 0;
 
   cudaGraphExec_t gexec = nullptr;
-  int graph_parity = -1;
+  std::vector<int> graph_curs;  // each active context's current buffer at capture
+  long long graph_launches_per = 0;
   int graph_steps = 16;  // even
 
   int blocks_per_sm[heat::kNumKinds] = {};
@@ -100,7 +116,16 @@ namespace {
 void drop_graph(heat_batch *b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
-  b->graph_parity = -1;
+  b->graph_curs.clear();
+}
+
+// Whether the captured graph's launches read the buffers every active
+// context currently holds.
+bool graph_matches(const heat_batch *b) {
+  if (!b->gexec || b->graph_curs.size() != b->active.size()) return false;
+  for (size_t a = 0; a < b->active.size(); ++a)
+    if (b->entries[b->active[a]].ctx->cur != b->graph_curs[a]) return false;
+  return true;
 }
 
 void release(heat_batch *b) {
@@ -113,6 +138,11 @@ void release(heat_batch *b) {
     if (b->join_ev[f]) cudaEventDestroy(b->join_ev[f]);
   }
   if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  if (b->solo_stream) {
+    cudaStreamSynchronize(b->solo_stream);
+    cudaStreamDestroy(b->solo_stream);
+  }
+  if (b->solo_join) cudaEventDestroy(b->solo_join);
   if (b->copy_stream) {
     cudaStreamSynchronize(b->copy_stream);
     cudaStreamDestroy(b->copy_stream);
@@ -187,14 +217,21 @@ const double kFormRate[heat::kNumForms] = {90.0, 80.0, 29.0, 200.0};
 int rebuild(heat_batch *b) {
   drop_graph(b);
   b->active.clear();
+  b->solo.clear();
   std::vector<heat::BatchGrid> grids;
   std::vector<heat::BatchTile> per_form[heat::kNumKinds];
   double work[heat::kNumKinds] = {};
   for (size_t e = 0; e < b->entries.size(); ++e) {
-    const heat_batch::Entry &en = b->entries[e];
+    heat_batch::Entry &en = b->entries[e];
     if (en.remaining <= 0) continue;
     const heat_ctx *c = en.ctx;
-    b->entries[e].base_steps = c->steps_done;
+    en.base_steps = c->steps_done;
+    const long long pts = (long long)(c->g.nx - 2) * (c->g.ny - 2) * (c->g.nz - 2);
+    en.solo = b->solo_points > 0 && pts >= b->solo_points;
+    if (en.solo) {
+      b->solo.push_back((int)e);
+      continue;
+    }
     const int form = heat::batch_form(c);
     const int kind = 2 * form + (grid_has_rhs(c) ? 1 : 0);
     const int gi = (int)grids.size();
@@ -211,6 +248,7 @@ int rebuild(heat_batch *b) {
     }
     work[kind] += (double)(c->g.nx - 2) * (c->g.ny - 2) * interior / kFormRate[form];
   }
+  b->active.insert(b->active.end(), b->solo.begin(), b->solo.end());
   std::vector<heat::BatchTile> tiles;
   double total = 0;
   b->nforms = 0;
@@ -273,34 +311,55 @@ void advance(heat_batch *b, long long n) {
   for (int e : b->active) {
     heat_batch::Entry &en = b->entries[e];
     en.ctx->steps_done += n;
-    if (n & 1) en.ctx->cur ^= 1;
+    if (en.solo ? heat::ctx_flips(en.ctx, n) : (n & 1)) en.ctx->cur ^= 1;
     en.remaining -= n;
   }
   b->since_build += n;
   b->batch_steps += n;
 }
 
+// The solo grids' n steps, one grid after another, on stream st.
+cudaError_t enqueue_solo(heat_batch *b, int n, cudaStream_t st, long long *launches) {
+  cudaError_t err = cudaSuccess;
+  for (size_t a = 0; a < b->solo.size() && err == cudaSuccess; ++a) {
+    heat_ctx *c = b->entries[b->solo[a]].ctx;
+    err = heat::enqueue_ctx_steps(c, c->cur, n, st, launches);
+  }
+  return err;
+}
+
 // Enqueue `n` steps starting at parity p: each form's kernel on its own side
 // stream (forked from and joined back to the batch stream) when several forms
-// are present, so a memory-bound and a compute-bound form share the SMs.
-cudaError_t enqueue_steps(heat_batch *b, int p, int n) {
+// are present, so a memory-bound and a compute-bound form share the SMs; the
+// solo grids on a further side stream.  *launches counts the kernels.
+cudaError_t enqueue_steps(heat_batch *b, int p, int n, long long *launches) {
   cudaError_t err = cudaSuccess;
-  if (b->nforms <= 1 || !b->concurrent) {
+  const int parts = b->nforms + (b->solo.empty() ? 0 : 1);
+  if (parts <= 1 || !b->concurrent) {
     for (int f = 0; f < heat::kNumKinds; ++f) {
       if (!b->tile_count[f]) continue;
       for (int s = 0; s < n && err == cudaSuccess; ++s)
         err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
                                  (p + s) & 1, b->form_blocks[f], b->stream);
+      *launches += n;
     }
+    if (err == cudaSuccess) err = enqueue_solo(b, n, b->stream, launches);
     return err;
   }
   err = cudaEventRecord(b->fork_ev, b->stream);
+  if (err == cudaSuccess && !b->solo.empty()) {
+    err = cudaStreamWaitEvent(b->solo_stream, b->fork_ev, 0);
+    if (err == cudaSuccess) err = enqueue_solo(b, n, b->solo_stream, launches);
+    if (err == cudaSuccess) err = cudaEventRecord(b->solo_join, b->solo_stream);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(b->stream, b->solo_join, 0);
+  }
   for (int f = 0; f < heat::kNumKinds && err == cudaSuccess; ++f) {
     if (!b->tile_count[f]) continue;
     err = cudaStreamWaitEvent(b->side[f], b->fork_ev, 0);
     for (int s = 0; s < n && err == cudaSuccess; ++s)
       err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
                                (p + s) & 1, b->form_blocks[f], b->side[f]);
+    *launches += n;
     if (err == cudaSuccess) err = cudaEventRecord(b->join_ev[f], b->side[f]);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(b->stream, b->join_ev[f], 0);
   }
@@ -313,12 +372,13 @@ void mark_table_use(heat_batch *b) {
 }
 
 int launch_plain(heat_batch *b, int n) {
-  if (enqueue_steps(b, (int)(b->since_build & 1), n) != cudaSuccess) {
+  long long nl = 0;
+  if (enqueue_steps(b, (int)(b->since_build & 1), n, &nl) != cudaSuccess) {
     cudaGetLastError();
     return HEAT_ECUDA;
   }
   mark_table_use(b);
-  b->launches += (long long)n * b->nforms;
+  b->launches += nl;
   advance(b, n);
   return HEAT_OK;
 }
@@ -331,7 +391,8 @@ int capture_graph(heat_batch *b) {
     return HEAT_ECUDA;
   }
   const int p = (int)(b->since_build & 1);
-  cudaError_t err = enqueue_steps(b, p, b->graph_steps);
+  long long nl = 0;
+  cudaError_t err = enqueue_steps(b, p, b->graph_steps, &nl);
   cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
   if (err != cudaSuccess || e2 != cudaSuccess || !graph) {
     if (graph) cudaGraphDestroy(graph);
@@ -345,7 +406,9 @@ int capture_graph(heat_batch *b) {
     cudaGetLastError();
     return HEAT_ECUDA;
   }
-  b->graph_parity = p;
+  b->graph_curs.clear();
+  for (int e : b->active) b->graph_curs.push_back(b->entries[e].ctx->cur);
+  b->graph_launches_per = nl;
   return HEAT_OK;
 }
 
@@ -377,6 +440,9 @@ int heat_batch_create(heat_batch **out, void *stream, unsigned flags) {
   for (int f = 0; f < heat::kNumKinds && ok; ++f)
     ok = cudaStreamCreateWithFlags(&b->side[f], cudaStreamNonBlocking) == cudaSuccess &&
          cudaEventCreateWithFlags(&b->join_ev[f], cudaEventDisableTiming) == cudaSuccess;
+  ok = ok && cudaStreamCreateWithFlags(&b->solo_stream, cudaStreamNonBlocking) == cudaSuccess &&
+       cudaEventCreateWithFlags(&b->solo_join, cudaEventDisableTiming) == cudaSuccess;
+  if (const char *ev = std::getenv("HEAT_BATCH_SOLO_POINTS")) b->solo_points = std::atoll(ev);
   if (!ok) {
     cudaGetLastError();
     release(b);
@@ -478,12 +544,14 @@ int batch_run(heat_batch *b, long long max_steps, long long *steps_taken, bool s
     if (m <= 0) break;
     const bool graphs = !(b->flags & HEAT_BATCH_NO_GRAPHS);
     if (graphs && m >= b->graph_steps) {
-      if (b->gexec && b->graph_parity != (int)(b->since_build & 1)) {
-        // the graph was captured at the other parity: one plain launch first
+      if (b->gexec && !graph_matches(b)) {
+        // the graph was captured with other current buffers: one plain step
+        // (table grids swap with step parity), else capture anew
         rc = launch_plain(b, 1);
         if (rc != HEAT_OK) break;
         ++done;
         --m;
+        if (!graph_matches(b)) drop_graph(b);
       }
       if (m >= b->graph_steps) {
         if (!b->gexec) {
@@ -498,7 +566,7 @@ int batch_run(heat_batch *b, long long max_steps, long long *steps_taken, bool s
             break;
           }
           b->graph_launches += 1;
-          b->launches += (long long)b->graph_steps * b->nforms;
+          b->launches += b->graph_launches_per;
           mark_table_use(b);
           advance(b, b->graph_steps);
           done += b->graph_steps;

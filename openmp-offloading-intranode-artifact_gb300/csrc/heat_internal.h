@@ -90,6 +90,13 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             const unsigned long long *K, const double *c0,
                             double *const cf[3], const heat_geom &g, int hw_rows,
                             cudaStream_t st);
+// n steps of context c from buffer `cur` on stream st with its own
+// single-grid kernels (two steps per launch where its form has them); the
+// context's bookkeeping is untouched.  ctx_flips gives the parity of buffer
+// swaps those n steps make (a two-step launch swaps once).
+cudaError_t enqueue_ctx_steps(heat_ctx *c, int cur, long long n, cudaStream_t st,
+                              long long *launches);
+int ctx_flips(const heat_ctx *c, long long n);
 
 // heat_fp32c.cu
 cudaError_t launch_fp32c(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,

@@ -130,3 +130,30 @@ def test_tuner_cache(H, tmp_path, monkeypatch):
     ent = [e for e in doc["entries"] if e["form"] == 3 and e["nz_max"] == 64]
     assert ent and ent[0]["kchunk"] >= 1 and ent[0]["glups"] > 0
     assert H.tune_lookup(H.HEAT_FP32C, 0, 40) == ent[0]["kchunk"]
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_solo_and_table_grids_mixed(H, monkeypatch, graphs):
+    """Grids above the solo threshold step with their single-grid kernels
+    (two FP32C steps per launch) beside the tile table; odd step counts and
+    runs cut into uneven pieces exercise the buffer-swap bookkeeping and the
+    graph-replay check.  Every grid equals its result alone."""
+    monkeypatch.setenv("HEAT_BATCH_SOLO_POINTS", "30000")
+    rng = random.Random(11)
+    specs = []
+    for idx, (_, prec, fl) in enumerate(FORMS * 2):
+        big = idx % 2 == 0
+        shape = tuple(rng.randint(36, 48) if big else rng.randint(10, 24) for _ in range(3))
+        specs.append((shape, 300 + idx, prec, fl, rng.choice([17, 33, 40, 51, 64])))
+    solvers = [make(H, sh, sd, p, f) for sh, sd, p, f, _ in specs]
+    with H.Batch(graphs=graphs) as b:
+        for s, spec in zip(solvers, specs):
+            b.add(s, spec[4])
+        total = 0
+        for piece in (5, 16, 1, 19, 2, 33, 100):
+            total += b.run(piece)
+        assert total == max(sp[4] for sp in specs)
+    for s, (sh, sd, p, f, n) in zip(solvers, specs):
+        assert bits_equal(s.field(), alone(H, sh, sd, p, f, n)), (sh, p, f, n)
+        assert s.stats()[0] == n
+        s.close()
