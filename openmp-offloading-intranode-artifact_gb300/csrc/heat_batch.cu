@@ -48,10 +48,12 @@ __device__ __forceinline__ void run_tile(const BatchGrid &g, size_t c, int kb, i
 // allocation (and occupancy) of its own column walk; the host launches one per
 // kind present.
 // Resident blocks per SM each kind is compiled for (caps its registers): the
-// memory-bound forms want many warps in flight, the integer walk needs room.
+// memory-bound forms want many warps in flight; the hybrid form takes 3 (80
+// registers, a few spills), as its single-grid kernel does -- 123 GLUP/s on
+// configuration 3's grids in the table alone, against 101 with 2.
 template <int FORM>
 struct MinBlocks {
-  static constexpr int value = FORM == kFormMix ? 2 : 4;
+  static constexpr int value = FORM == kFormMix ? 3 : 4;
 };
 
 template <int FORM, bool RHS>
