@@ -26,6 +26,8 @@ DRV = PKG / "heatdrv"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                       "-I", str(ROOT / "include"), "-I", str(CSRC)]
+# Extra nvcc flags for every CUDA unit (e.g. -D switches), from the environment.
+NVCC_COMMON += os.environ.get("HEAT_NVCC_EXTRA", "").split()
 # Per-unit extra flags.
 UNIT_FLAGS = {
     "heat_fp64_exact.cu": ["--fmad=false", "--prec-div=true", "--prec-sqrt=true", "--ftz=false"],
