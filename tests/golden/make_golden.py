@@ -34,7 +34,7 @@ sys.path.insert(0, str(ROOT / "oracle"))
 import heat_oracle as orc  # noqa: E402
 
 SMALL = [(5, 3), (12, 10), (12, 50), (17, 20), (24, 37)]
-LARGE = [(51, 100), (64, 100), (128, 50), (256, 100)]
+LARGE = [(n, s) for n in (51, 64, 128, 256) for s in (1, 50, 100)]
 
 
 def sha(a: np.ndarray) -> str:
