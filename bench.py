@@ -205,6 +205,23 @@ def profile_traffic():
     return None
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of every rank's x (the slowest rank's time); x itself
+    without a process group."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(updates_per_rank, world, t_max_s):
+    """Whole-job GLUP/s of `world` independent replicas: every rank's updates
+    over the slowest rank's time."""
+    return updates_per_rank * world / t_max_s / 1e9
+
+
 def our_arm(a):
     import numpy as np
     import torch
@@ -266,13 +283,9 @@ def our_arm(a):
     ms32 = e0.elapsed_time(e1)
     s32.close()
     fp32c_value = updates(n, ts) / (ms32 * 1e-3) / 1e9
-    t_max = ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
+    t_max = max_over_ranks(ms, dist, "cuda")
     upd = updates(n, ts) * a.steps
-    value = upd * world / (t_max * 1e-3) / 1e9
+    value = replica_value(upd, world, t_max * 1e-3)
     launch_ms = ms / (a.steps * ts)
     achieved_gbs = updates(n, 1) * BYTES_PER_UPDATE / (launch_ms * 1e-3) / 1e9
 
@@ -295,12 +308,8 @@ def our_arm(a):
             e2e_t = 0.0
         else:
             e2e_t += t1 - t0
-    e2e_s = e2e_t / e2e_steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = updates(n, ts) * world / e2e_s / 1e9
+    e2e_s = max_over_ranks(e2e_t / e2e_steps, dist, "cuda")
+    e2e_value = replica_value(updates(n, ts), world, e2e_s)
 
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
