@@ -28,6 +28,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -385,7 +386,11 @@ int heat_server_create(heat_server **out, size_t budget_bytes, int tick_steps, i
     delete s;
     return HEAT_ECUDA;
   }
-  int rc = heat_batch_create(&s->batch, s->stream, 0);
+  // HEAT_SERVER_BATCH_FLAGS: heat_batch_create flags of the server's batch
+  // (e.g. 1 = no graphs); a tuning knob.
+  unsigned bflags = 0;
+  if (const char *ev = std::getenv("HEAT_SERVER_BATCH_FLAGS")) bflags = (unsigned)std::atoi(ev);
+  int rc = heat_batch_create(&s->batch, s->stream, bflags);
   if (rc != HEAT_OK) {
     cudaStreamDestroy(s->stream);
     delete s;
