@@ -24,6 +24,7 @@ from pathlib import Path
 
 sys.path.insert(0, str(Path(__file__).resolve().parent))
 import heat_ctypes as H  # noqa: E402
+from clocks import ClockSampler  # noqa: E402
 
 
 def main() -> None:
@@ -66,10 +67,11 @@ def main() -> None:
     for s, sp in zip(solvers, specs):
         batch.add(s, sp["steps"])
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    taken = batch.run()
-    e1.record(stream)
-    e1.synchronize()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record(stream)
+        taken = batch.run()
+        e1.record(stream)
+        e1.synchronize()
     ms = e0.elapsed_time(e1)
     launches, graphs, _ = batch.stats()
     batch.close()
@@ -78,7 +80,8 @@ def main() -> None:
            "updates": updates, "batch_ms": round(ms, 2), "batch_glups": round(updates / (ms * 1e-3) / 1e9, 2),
            "batch_steps": taken, "kernel_launches": launches, "graph_launches": graphs,
            "tune_s": round(tune_s, 2), "setup_s": round(setup_s, 2),
-           "kchunks": {str(n): H.tune_lookup(p, 0, n) for p in (0, 1) for n in (64, 128, 256, 384)}}
+           "kchunks": {str(n): H.tune_lookup(p, 0, n) for p in (0, 1) for n in (64, 128, 256, 384)},
+           "clocks": clk.summary()}
     if not a.skip_sequential:
         # the same work, one context at a time with heat_step (fresh contexts)
         seq_ms = 0.0

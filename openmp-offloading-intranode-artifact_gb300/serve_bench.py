@@ -26,6 +26,7 @@ from pathlib import Path
 
 sys.path.insert(0, str(Path(__file__).resolve().parent))
 import heat_ctypes as H  # noqa: E402
+from clocks import ClockSampler  # noqa: E402
 
 
 def log_uniform(rng: random.Random, lo: float, hi: float) -> float:
@@ -59,14 +60,15 @@ def main() -> None:
 
     srv = H.Server(budget_bytes=int(a.budget_gb * (1 << 30)), tick_steps=a.tick,
                    prep_threads=a.prep_threads)
-    t0 = time.perf_counter()
-    for (ta, nx, ny, nz, steps, prec, seed) in reqs:
-        delay = ta - (time.perf_counter() - t0)
-        if delay > 0:
-            time.sleep(delay)
-        srv.submit(nx, ny, nz, steps, precision=prec, cfg=0, seed=seed)
-    srv.wait_idle()
-    wall = time.perf_counter() - t0
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for (ta, nx, ny, nz, steps, prec, seed) in reqs:
+            delay = ta - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            srv.submit(nx, ny, nz, steps, precision=prec, cfg=0, seed=seed)
+        srv.wait_idle()
+        wall = time.perf_counter() - t0
     res = srv.poll(max_results=a.requests + 16)
     st = srv.stats()
     srv.close()
@@ -86,7 +88,7 @@ def main() -> None:
            "p50_ms_fp32c": pct(lat32, 0.5), "p99_ms_fp32c": pct(lat32, 0.99),
            "glups": round(st["glups"], 2), "completed": st["completed"], "rejected": st["rejected"],
            "peak_gb": round(st["peak_bytes"] / (1 << 30), 2), "batch_steps": st["batch_steps"],
-           "kernel_launches": st["kernel_launches"]}
+           "kernel_launches": st["kernel_launches"], "clocks": clk.summary()}
     print(json.dumps(out), flush=True)
 
 
