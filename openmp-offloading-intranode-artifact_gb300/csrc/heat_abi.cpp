@@ -212,9 +212,10 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
   TRY(dalloc(&c->partials, 2 * heat::kNormBlocks + 2, c->stream));
   c->n_partials = heat::kNormBlocks;
   TRY(dalloc(&c->err, 1, c->stream));
+  // Padding columns are zeroed; without padding the uploads cover everything.
   if (cudaMemsetAsync(c->err, 0, sizeof(int), c->stream) != cudaSuccess ||
-      cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
-      cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess) {
+      (g.pitch != g.nx && (cudaMemsetAsync(c->u[0], 0, bytes, c->stream) != cudaSuccess ||
+                           cudaMemsetAsync(kap, 0, bytes, c->stream) != cudaSuccess))) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemset");
     goto done;
   }
@@ -229,7 +230,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
   }
   if (d->rhs) {
     TRY(dalloc(&c->rhs, g.elems, c->stream));
-    if (cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
+    if (g.pitch != g.nx && cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaMemset");
       goto done;
     }

@@ -65,12 +65,13 @@ __global__ void k_widen(double *__restrict__ u, const float *__restrict__ v,
 __global__ void k_f32_weights(float *__restrict__ wx, float *__restrict__ wy,
                               float *__restrict__ wz, const double *__restrict__ kap, int nx,
                               int ny, int nz, int P, size_t S, double factor) {
-  size_t total = S * nz;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total;
-       c += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(c % P);
-    int j = (int)((c / P) % ny);
-    int k = (int)(c / S);
+  // One row (j, k) per block iteration, its points across the threads: no
+  // per-point index division.
+  const long rows = (long)ny * nz;
+  for (long r = blockIdx.x; r < rows; r += gridDim.x)
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const int j = (int)(r % ny), k = (int)(r / ny);
+    const size_t c = (size_t)k * S + (size_t)j * P + i;
     bool in = i < nx;
     double kc = in ? kap[c] : 0.0;
     wx[c] = (i + 1 < nx) ? (float)(factor * (kc + kap[c + 1])) : 0.0f;

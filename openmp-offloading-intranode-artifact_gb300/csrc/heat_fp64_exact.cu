@@ -99,12 +99,13 @@ __global__ void __launch_bounds__(TX *TY)
 __global__ void k_face_sums(double *__restrict__ kx, double *__restrict__ ky,
                             double *__restrict__ kz, const double *__restrict__ kap,
                             int nx, int ny, int nz, int P, size_t S) {
-  size_t total = S * nz;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total;
-       c += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(c % P);
-    int j = (int)((c / P) % ny);
-    int k = (int)(c / S);
+  // One row (j, k) per block iteration, its points across the threads: no
+  // per-point index division.
+  const long rows = (long)ny * nz;
+  for (long r = blockIdx.x; r < rows; r += gridDim.x)
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const int j = (int)(r % ny), k = (int)(r / ny);
+    const size_t c = (size_t)k * S + (size_t)j * P + i;
     kx[c] = (i + 1 < nx) ? __dadd_rn(kap[c], kap[c + 1]) : 0.0;
     ky[c] = (j + 1 < ny && i < nx) ? __dadd_rn(kap[c], kap[c + P]) : 0.0;
     kz[c] = (k + 1 < nz && i < nx) ? __dadd_rn(kap[c], kap[c + S]) : 0.0;

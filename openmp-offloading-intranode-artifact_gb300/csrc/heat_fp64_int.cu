@@ -47,12 +47,13 @@ __global__ void __launch_bounds__(TX *TYB, MINB)
 __global__ void k_kq_setup(u64 *__restrict__ K, int *__restrict__ bad,
                            const double *__restrict__ kap, int nx, int ny, int nz, int P,
                            size_t S, double factor) {
-  size_t total = S * nz;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total;
-       c += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(c % P);
-    int j = (int)((c / P) % ny);
-    int k = (int)(c / S);
+  // One row (j, k) per block iteration, its points across the threads: no
+  // per-point index division.
+  const long rows = (long)ny * nz;
+  for (long r = blockIdx.x; r < rows; r += gridDim.x)
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    const int j = (int)(r % ny), k = (int)(r / ny);
+    const size_t c = (size_t)k * S + (size_t)j * P + i;
     if (i >= nx) {
       K[c] = 0;
       continue;
