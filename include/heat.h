@@ -213,6 +213,7 @@ typedef struct heat_server_summary {
   double updates, busy_ms;
   size_t budget_bytes, bytes_in_use, peak_bytes;
   long long batch_steps, kernel_launches;
+  double gpu_ms;           /* device time inside ticks (gaps: GPU waiting for the host) */
 } heat_server_summary;
 
 int heat_server_create(heat_server **out, size_t budget_bytes, int tick_steps, int prep_threads);

@@ -77,7 +77,7 @@ class HeatServerStats(C.Structure):
                 ("max_ms", C.c_double), ("glups", C.c_double), ("updates", C.c_double),
                 ("busy_ms", C.c_double), ("budget_bytes", C.c_size_t), ("bytes_in_use", C.c_size_t),
                 ("peak_bytes", C.c_size_t), ("batch_steps", C.c_longlong),
-                ("kernel_launches", C.c_longlong)]
+                ("kernel_launches", C.c_longlong), ("gpu_ms", C.c_double)]
 
 # Every symbol include/heat.h declares, with its ctypes signature.
 SIGNATURES = {

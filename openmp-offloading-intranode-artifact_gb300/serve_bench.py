@@ -88,7 +88,9 @@ def main() -> None:
            "p50_ms_fp32c": pct(lat32, 0.5), "p99_ms_fp32c": pct(lat32, 0.99),
            "glups": round(st["glups"], 2), "completed": st["completed"], "rejected": st["rejected"],
            "peak_gb": round(st["peak_bytes"] / (1 << 30), 2), "batch_steps": st["batch_steps"],
-           "kernel_launches": st["kernel_launches"], "clocks": clk.summary()}
+           "kernel_launches": st["kernel_launches"],
+           "gpu_busy_frac": round(st["gpu_ms"] * 1e-3 / wall, 3) if wall > 0 else None,
+           "clocks": clk.summary()}
     print(json.dumps(out), flush=True)
 
 
