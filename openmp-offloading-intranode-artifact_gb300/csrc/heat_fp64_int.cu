@@ -39,6 +39,47 @@ __global__ void __launch_bounds__(TX *TYB, MINB)
     walk::walk_int<RHS>(un, reinterpret_cast<const u64 *>(u), rhs, K, P, S, c, kb, ke);
 }
 
+// The hw_rows = 4 split as one launch of 4 blocks per SM (64 registers per
+// thread) whose two warpgroups run separate code: warps 0-3 the FP64 rows,
+// warps 4-7 the integer rows.  Each warpgroup starts with setmaxnreg at the
+// launch count (64): no registers move between them, but the instruction
+// bounds each region for ptxas's allocator, which then spills half as much
+// (76 B against 152 B without it).  Measured at 512^3: 111 GLUP/s against 99
+// for the same kernel without setmaxnreg and 102-105 for k_fast_mix at 3
+// blocks per SM; moving registers from the FP64 to the integer warpgroup
+// (56/72, 48/80) or 3 blocks per SM with any split measured 83-105.  The host
+// launches it only when the compiled register count is kWsRegs, since a
+// setmaxnreg.inc above the launch count would wait for registers forever.
+constexpr int kWsRegs = 64;
+
+template <bool RHS>
+__global__ void __launch_bounds__(256, 4)
+    k_fast_ws(double *__restrict__ un, const double *__restrict__ u,
+              const double *__restrict__ rhs, const u64 *__restrict__ K,
+              const double *__restrict__ c0, const double *__restrict__ cx,
+              const double *__restrict__ cy, const double *__restrict__ cz, int nx, int ny,
+              int nz, int P, size_t S, int kchunk) {
+  if (threadIdx.y < 4) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    const int i = 1 + blockIdx.x * TX + threadIdx.x;
+    const int j = 1 + blockIdx.y * TY + threadIdx.y;
+    const int kb = 1 + blockIdx.z * kchunk;
+    const int ke = min(kb + kchunk, nz - 1);
+    if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
+    const size_t c = (size_t)kb * S + (size_t)j * P + i;
+    walk::walk_hw<RHS>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
+  } else {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    const int i = 1 + blockIdx.x * TX + threadIdx.x;
+    const int j = 1 + blockIdx.y * TY + threadIdx.y;
+    const int kb = 1 + blockIdx.z * kchunk;
+    const int ke = min(kb + kchunk, nz - 1);
+    if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
+    const size_t c = (size_t)kb * S + (size_t)j * P + i;
+    walk::walk_int<RHS>(un, reinterpret_cast<const u64 *>(u), rhs, K, P, S, c, kb, ke);
+  }
+}
+
 // K[c] = round(factor * kappa[c] * 2^64) from the error-free product
 // p + q = factor * kappa (q = fma(factor, kappa, -p)); padding columns get 0.
 // bad[0] is set when the fixed-point form cannot represent the problem:
@@ -116,6 +157,36 @@ void launch_mix_shape(double *u_new, const double *u_old, const double *rhs,
       hw_rows);
 }
 
+// True when k_fast_ws<RHS> compiled to exactly kWsRegs registers per thread
+// (checked once per process).
+template <bool RHS>
+bool ws_usable() {
+  static const bool ok = [] {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k_fast_ws<RHS>) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return a.numRegs == kWsRegs;
+  }();
+  return ok;
+}
+
+template <bool RHS>
+void launch_ws(double *u_new, const double *u_old, const double *rhs,
+               const unsigned long long *K, const double *c0, double *const cf[3],
+               const heat_geom &g, cudaStream_t st) {
+  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
+  long want = 152L * 16;
+  long chunks = (want + tiles - 1) / tiles;
+  int interior = g.nz - 2;
+  int kc = (int)((interior + chunks - 1) / chunks);
+  kc = std::max(8, std::min(kc, interior));
+  dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
+  k_fast_ws<RHS><<<gr, dim3(TX, TY), 0, st>>>(u_new, u_old, rhs, K, c0, cf[0], cf[1], cf[2],
+                                              g.nx, g.ny, g.nz, g.pitch, g.plane, kc);
+}
+
 }  // namespace
 
 cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rhs,
@@ -124,10 +195,13 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             cudaStream_t st) {
   if (hw_rows < 0) hw_rows = 0;
   if (hw_rows > 8) hw_rows = 8;
-  // Launch shape: 8-row blocks with registers capped for 3 resident blocks
-  // per SM (a few spills, more warps to hide the integer walk's load
-  // latency): 101 GLUP/s at 512^3 against 94 for 2 blocks per SM.
-  if (rhs)
+  // Default split without a source term: k_fast_ws.  Otherwise 8-row blocks
+  // with registers capped for 3 resident blocks per SM (a few spills, more
+  // warps to hide the integer walk's load latency): 101 GLUP/s at 512^3
+  // against 94 for 2 blocks per SM.
+  if (!rhs && hw_rows == 4 && ws_usable<false>())
+    launch_ws<false>(u_new, u_old, rhs, K, c0, cf, g, st);
+  else if (rhs)
     launch_mix_shape<true, 8, 2>(u_new, u_old, rhs, K, c0, cf, g, hw_rows, st);
   else
     launch_mix_shape<false, 8, 3>(u_new, u_old, rhs, K, c0, cf, g, hw_rows, st);
