@@ -72,6 +72,46 @@ __global__ void __launch_bounds__(TX *TY, MinBlocks<FORM>::value)
   }
 }
 
+// The default FP64 form's tiles (hw_rows = 4, no source term) as the
+// single-grid k_fast_ws runs them: 4 blocks per SM, warps 0-3 walk the tile's
+// FP64 rows and warps 4-7 its integer rows in separate code, each warpgroup
+// starting with setmaxnreg at the launch count (64) so that ptxas allocates
+// the two walks separately.
+constexpr int kWsRegs = 64;
+
+__global__ void __launch_bounds__(TX *TY, 4)
+    k_batch_ws(const BatchGrid *__restrict__ grids, const BatchTile *__restrict__ tiles,
+               int ntiles, int flip) {
+  if (threadIdx.y < 4) {
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const BatchTile tl = tiles[t];
+      const BatchGrid &g = grids[tl.grid];
+      const int i = 1 + tl.tx * TX + threadIdx.x;
+      const int j = 1 + tl.ty * TY + threadIdx.y;
+      if (i >= g.nx - 1 || j >= g.ny - 1) continue;
+      const int src = g.cur ^ flip, dst = src ^ 1;
+      const size_t c = (size_t)tl.k0 * g.S + (size_t)j * g.P + i;
+      walk::walk_hw<false>((double *)g.f[dst], (const double *)g.f[src], nullptr,
+                           (const double *)g.w[0], (const double *)g.w[1], (const double *)g.w[2],
+                           (const double *)g.w[3], g.P, g.S, c, tl.k0, tl.k1);
+    }
+  } else {
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+      const BatchTile tl = tiles[t];
+      const BatchGrid &g = grids[tl.grid];
+      const int i = 1 + tl.tx * TX + threadIdx.x;
+      const int j = 1 + tl.ty * TY + threadIdx.y;
+      if (i >= g.nx - 1 || j >= g.ny - 1) continue;
+      const int src = g.cur ^ flip, dst = src ^ 1;
+      const size_t c = (size_t)tl.k0 * g.S + (size_t)j * g.P + i;
+      walk::walk_int<false>((double *)g.f[dst], (const u64 *)g.f[src], nullptr, g.kq, g.P, g.S, c,
+                            tl.k0, tl.k1);
+    }
+  }
+}
+
 template <int FORM, bool RHS>
 int occupancy() {
   int nb = 0;
@@ -93,6 +133,10 @@ cudaError_t launch_batch(int kind, const BatchGrid *grids, const BatchTile *tile
   case 2 * (F) + (R):                                                           \
     k_batch<(F), (R)><<<blocks, b, 0, st>>>(grids, tiles, ntiles, flip);        \
     break;
+  if (kind == 2 * kFormMixWs) {
+    k_batch_ws<<<blocks, b, 0, st>>>(grids, tiles, ntiles, flip);
+    return cudaGetLastError();
+  }
   switch (kind) {
     HEAT_BATCH_CASE(kFormMix, 0)
     HEAT_BATCH_CASE(kFormMix, 1)
@@ -108,7 +152,28 @@ cudaError_t launch_batch(int kind, const BatchGrid *grids, const BatchTile *tile
   return cudaGetLastError();
 }
 
+bool batch_ws_usable() {
+  static const bool ok = [] {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k_batch_ws) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return a.numRegs == kWsRegs;
+  }();
+  return ok;
+}
+
 int batch_blocks_per_sm(int kind) {
+  if (kind == 2 * kFormMixWs) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_ws, TX * TY, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return 1;
+    }
+    return nb > 0 ? nb : 1;
+  }
+  if (kind == 2 * kFormMixWs + 1) return 1;  // not produced (source-term grids use kFormMix)
   switch (kind) {
     case 2 * kFormMix: return occupancy<kFormMix, false>();
     case 2 * kFormMix + 1: return occupancy<kFormMix, true>();

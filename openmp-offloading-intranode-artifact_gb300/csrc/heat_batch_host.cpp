@@ -101,7 +101,8 @@ int batch_form(const heat_ctx *c) {
   if (c->precision == HEAT_FP32C) return kFormF32c;
   if (c->flags & HEAT_NAIVE) return -1;
   if (c->flags & HEAT_BITEXACT) return kFormExact;
-  return c->kq ? kFormMix : kFormHw;
+  if (!c->kq) return kFormHw;
+  return (c->hw_rows == 4 && !c->rhs && batch_ws_usable()) ? kFormMixWs : kFormMix;
 }
 
 void batch_set_kchunk_override(heat_batch *b, int kchunk) {
@@ -212,7 +213,7 @@ heat::BatchGrid describe(const heat_ctx *c, int form) {
 
 // Throughput guesses (GLUP/s on GB300) used only to split the SMs between
 // forms that run side by side.
-const double kFormRate[heat::kNumForms] = {90.0, 80.0, 29.0, 200.0};
+const double kFormRate[heat::kNumForms] = {100.0, 80.0, 29.0, 200.0, 110.0};
 
 int rebuild(heat_batch *b) {
   drop_graph(b);
@@ -238,7 +239,9 @@ int rebuild(heat_batch *b) {
     grids.push_back(describe(c, form));
     b->active.push_back((int)e);
     const int interior = c->g.nz - 2;
-    int kc = b->kchunk_override > 0 ? b->kchunk_override : heat::tuned_kchunk(form, c->g.nz);
+    // the warpgroup-split form walks tiles as the hybrid one does: same z-chunk
+    const int tform = form == heat::kFormMixWs ? heat::kFormMix : form;
+    int kc = b->kchunk_override > 0 ? b->kchunk_override : heat::tuned_kchunk(tform, c->g.nz);
     kc = std::max(1, std::min(kc, interior));
     const int ntx = (c->g.nx - 2 + 31) / 32, nty = (c->g.ny - 2 + 7) / 8;
     for (int k0 = 1; k0 < c->g.nz - 1; k0 += kc) {

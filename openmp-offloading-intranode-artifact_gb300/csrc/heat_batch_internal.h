@@ -11,6 +11,7 @@ enum BatchForm : int {
   kFormHw = 1,     // default FP64 on the FP64 pipe only
   kFormExact = 2,  // bit-exact FP64 (face kappa sums)
   kFormF32c = 3,   // FP32-compensated
+  kFormMixWs = 4,  // default FP64, hw_rows = 4, no source term: warpgroup-split kernel
 };
 
 // One grid of a batch as the kernel sees it.  f[b] / cr[b] are the two field
@@ -39,13 +40,16 @@ struct BatchTile {
   int k0, k1;
 };
 
-constexpr int kNumForms = 4;
+constexpr int kNumForms = 5;
 // A kernel kind is (form, source term): kind = 2 * form + (rhs != NULL).
 constexpr int kNumKinds = 2 * kNumForms;
 // Launch the batch kernel of one kind over `ntiles` tiles (all of that kind).
 cudaError_t launch_batch(int kind, const BatchGrid *grids, const BatchTile *tiles, int ntiles,
                          int flip, int blocks, cudaStream_t st);
 int batch_blocks_per_sm(int kind);
+// Whether the warpgroup-split table kernel compiled to the register count
+// its setmaxnreg bounds assume (else kFormMix is used instead).
+bool batch_ws_usable();
 
 // Form of a context in the batch kernel, or -1 if the batch cannot run it.
 int batch_form(const heat_ctx *c);
