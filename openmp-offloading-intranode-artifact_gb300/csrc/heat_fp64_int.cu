@@ -52,15 +52,15 @@ __global__ void __launch_bounds__(TX *TYB, MINB)
 // setmaxnreg.inc above the launch count would wait for registers forever.
 constexpr int kWsRegs = 64;
 
-template <bool RHS>
-__global__ void __launch_bounds__(256, 4)
+template <bool RHS, int MINB = 4, int REGS = kWsRegs>
+__global__ void __launch_bounds__(256, MINB)
     k_fast_ws(double *__restrict__ un, const double *__restrict__ u,
               const double *__restrict__ rhs, const u64 *__restrict__ K,
               const double *__restrict__ c0, const double *__restrict__ cx,
               const double *__restrict__ cy, const double *__restrict__ cz, int nx, int ny,
               int nz, int P, size_t S, int kchunk) {
   if (threadIdx.y < 4) {
-    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;\n" ::"n"(REGS));
     const int i = 1 + blockIdx.x * TX + threadIdx.x;
     const int j = 1 + blockIdx.y * TY + threadIdx.y;
     const int kb = 1 + blockIdx.z * kchunk;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(256, 4)
     const size_t c = (size_t)kb * S + (size_t)j * P + i;
     walk::walk_hw<RHS>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
   } else {
-    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(kWsRegs));
+    asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(REGS));
     const int i = 1 + blockIdx.x * TX + threadIdx.x;
     const int j = 1 + blockIdx.y * TY + threadIdx.y;
     const int kb = 1 + blockIdx.z * kchunk;
@@ -159,20 +159,20 @@ void launch_mix_shape(double *u_new, const double *u_old, const double *rhs,
 
 // True when k_fast_ws<RHS> compiled to exactly kWsRegs registers per thread
 // (checked once per process).
-template <bool RHS>
+template <bool RHS, int MINB = 4, int REGS = kWsRegs>
 bool ws_usable() {
   static const bool ok = [] {
     cudaFuncAttributes a;
-    if (cudaFuncGetAttributes(&a, k_fast_ws<RHS>) != cudaSuccess) {
+    if (cudaFuncGetAttributes(&a, k_fast_ws<RHS, MINB, REGS>) != cudaSuccess) {
       cudaGetLastError();
       return false;
     }
-    return a.numRegs == kWsRegs;
+    return a.numRegs == REGS;
   }();
   return ok;
 }
 
-template <bool RHS>
+template <bool RHS, int MINB = 4, int REGS = kWsRegs>
 void launch_ws(double *u_new, const double *u_old, const double *rhs,
                const unsigned long long *K, const double *c0, double *const cf[3],
                const heat_geom &g, cudaStream_t st) {
@@ -183,8 +183,9 @@ void launch_ws(double *u_new, const double *u_old, const double *rhs,
   int kc = (int)((interior + chunks - 1) / chunks);
   kc = std::max(8, std::min(kc, interior));
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
-  k_fast_ws<RHS><<<gr, dim3(TX, TY), 0, st>>>(u_new, u_old, rhs, K, c0, cf[0], cf[1], cf[2],
-                                              g.nx, g.ny, g.nz, g.pitch, g.plane, kc);
+  k_fast_ws<RHS, MINB, REGS><<<gr, dim3(TX, TY), 0, st>>>(u_new, u_old, rhs, K, c0, cf[0], cf[1],
+                                                          cf[2], g.nx, g.ny, g.nz, g.pitch,
+                                                          g.plane, kc);
 }
 
 }  // namespace
@@ -195,12 +196,17 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             cudaStream_t st) {
   if (hw_rows < 0) hw_rows = 0;
   if (hw_rows > 8) hw_rows = 8;
-  // Default split without a source term: k_fast_ws.  Otherwise 8-row blocks
-  // with registers capped for 3 resident blocks per SM (a few spills, more
-  // warps to hide the integer walk's load latency): 101 GLUP/s at 512^3
-  // against 94 for 2 blocks per SM.
+  // Default split (hw_rows = 4): k_fast_ws.  Other splits: 8-row blocks with
+  // registers capped for 3 resident blocks per SM (a few spills, more warps
+  // to hide the integer walk's load latency): 101 GLUP/s at 512^3 against 94
+  // for 2 blocks per SM.
+  // With a source term the walks need more registers: the same split at 3
+  // blocks per SM (80 registers, no spills) runs the reference problem at 97
+  // GLUP/s (512^3) against 74 for k_fast_mix and 78 at 4 blocks per SM.
   if (!rhs && hw_rows == 4 && ws_usable<false>())
     launch_ws<false>(u_new, u_old, rhs, K, c0, cf, g, st);
+  else if (rhs && hw_rows == 4 && ws_usable<true, 3, 80>())
+    launch_ws<true, 3, 80>(u_new, u_old, rhs, K, c0, cf, g, st);
   else if (rhs)
     launch_mix_shape<true, 8, 2>(u_new, u_old, rhs, K, c0, cf, g, hw_rows, st);
   else
