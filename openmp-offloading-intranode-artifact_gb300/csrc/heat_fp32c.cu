@@ -86,23 +86,13 @@ __global__ void k_to_f32(float *__restrict__ o, const double *__restrict__ a, si
     o[p] = (float)a[p];
 }
 
-int choose_kchunk(const heat_geom &g) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
-  long want = 152L * 16;
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kchunk = (int)((interior + chunks - 1) / chunks);
-  if (kchunk < 8) kchunk = 8;
-  if (kchunk > interior) kchunk = interior;
-  return kchunk;
-}
 
 }  // namespace
 
 cudaError_t launch_fp32c(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
                          float *const w[3], const float *rhs, const heat_geom &g,
                          cudaStream_t st) {
-  int kc = choose_kchunk(g);
+  int kc = plane_chunk(g, TX, TY);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   dim3 b(TX, TY);
   if (rhs)

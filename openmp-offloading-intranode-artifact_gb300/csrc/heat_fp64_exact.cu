@@ -112,16 +112,6 @@ __global__ void k_face_sums(double *__restrict__ kx, double *__restrict__ ky,
   }
 }
 
-int choose_kchunk(const heat_geom &g) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
-  long want = 152L * 16;  // resident-block target across the SMs
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kchunk = (int)((interior + chunks - 1) / chunks);
-  if (kchunk < 8) kchunk = 8;
-  if (kchunk > interior) kchunk = interior;
-  return kchunk;
-}
 
 dim3 zgrid(const heat_geom &g, int kchunk) {
   return dim3((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY,
@@ -146,7 +136,7 @@ cudaError_t launch_naive(double *u_new, const double *u_old, const double *rhs,
 cudaError_t launch_exact_raw(double *u_new, const double *u_old, const double *rhs,
                              const double *kappa, const heat_geom &g, double factor,
                              cudaStream_t st) {
-  int kc = choose_kchunk(g);
+  int kc = plane_chunk(g, TX, TY);
   dim3 gr = zgrid(g, kc), b(TX, TY);
   if (rhs)
     k_exact_raw<true><<<gr, b, 0, st>>>(u_new, u_old, rhs, kappa, g.nx, g.ny, g.nz, g.pitch,
@@ -160,7 +150,7 @@ cudaError_t launch_exact_raw(double *u_new, const double *u_old, const double *r
 cudaError_t launch_exact_faces(double *u_new, const double *u_old, const double *rhs,
                                double *const ks[3], const heat_geom &g, double factor,
                                cudaStream_t st) {
-  int kc = choose_kchunk(g);
+  int kc = plane_chunk(g, TX, TY);
   dim3 gr = zgrid(g, kc), b(TX, TY);
   if (rhs)
     k_exact_faces<true><<<gr, b, 0, st>>>(u_new, u_old, rhs, ks[0], ks[1], ks[2], g.nx, g.ny,

@@ -61,16 +61,6 @@ __global__ void __launch_bounds__(TX *TY)
   walk::walk_hw<RHS>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
 }
 
-int choose_kchunk(const heat_geom &g) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
-  long want = 152L * 16;
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kchunk = (int)((interior + chunks - 1) / chunks);
-  if (kchunk < 8) kchunk = 8;
-  if (kchunk > interior) kchunk = interior;
-  return kchunk;
-}
 
 }  // namespace
 
@@ -85,7 +75,7 @@ cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
                         const double *c0, double *const cf[3], const heat_geom &g,
                         cudaStream_t st, bool hw_only) {
   (void)hw_only;
-  int kc = choose_kchunk(g);
+  int kc = plane_chunk(g, TX, TY);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   dim3 b(TX, TY);
   if (rhs)

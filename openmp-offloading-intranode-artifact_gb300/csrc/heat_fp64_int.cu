@@ -119,16 +119,6 @@ __global__ void k_kq_setup(u64 *__restrict__ K, int *__restrict__ bad,
   }
 }
 
-int choose_kchunk(const heat_geom &g) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
-  long want = 152L * 16;
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kchunk = (int)((interior + chunks - 1) / chunks);
-  if (kchunk < 8) kchunk = 8;
-  if (kchunk > interior) kchunk = interior;
-  return kchunk;
-}
 
 }  // namespace
 
@@ -144,13 +134,7 @@ template <bool RHS, int TYB, int MINB>
 void launch_mix_shape(double *u_new, const double *u_old, const double *rhs,
                       const unsigned long long *K, const double *c0, double *const cf[3],
                       const heat_geom &g, int hw_rows, cudaStream_t st) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TYB - 1) / TYB);
-  long want = 152L * 16 * (TY / TYB);
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kc = (int)((interior + chunks - 1) / chunks);
-  kc = std::max(8, std::min(kc, interior));
-  if (kc > interior) kc = interior;
+  const int kc = plane_chunk(g, TX, TYB, 152L * 16 * (TY / TYB));
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TYB - 1) / TYB, (g.nz - 2 + kc - 1) / kc);
   k_fast_mix<RHS, TYB, MINB><<<gr, dim3(TX, TYB), 0, st>>>(
       u_new, u_old, rhs, K, c0, cf[0], cf[1], cf[2], g.nx, g.ny, g.nz, g.pitch, g.plane, kc,
@@ -176,12 +160,7 @@ template <bool RHS, int MINB = 4, int REGS = kWsRegs>
 void launch_ws(double *u_new, const double *u_old, const double *rhs,
                const unsigned long long *K, const double *c0, double *const cf[3],
                const heat_geom &g, cudaStream_t st) {
-  long tiles = (long)((g.nx - 2 + TX - 1) / TX) * ((g.ny - 2 + TY - 1) / TY);
-  long want = 152L * 16;
-  long chunks = (want + tiles - 1) / tiles;
-  int interior = g.nz - 2;
-  int kc = (int)((interior + chunks - 1) / chunks);
-  kc = std::max(8, std::min(kc, interior));
+  const int kc = plane_chunk(g, TX, TY);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   k_fast_ws<RHS, MINB, REGS><<<gr, dim3(TX, TY), 0, st>>>(u_new, u_old, rhs, K, c0, cf[0], cf[1],
                                                           cf[2], g.nx, g.ny, g.nz, g.pitch,

@@ -61,6 +61,20 @@ namespace heat {
 
 constexpr int kNormBlocks = 152 * 4;   // partial-sum blocks of the norm pass
 
+// Planes per block for a launch of (tile_x x tile_y)-column tiles over the
+// grid's interior: enough z-chunks that tiles x chunks reaches `want` blocks
+// (16 per SM of GB300's 152 by default), at least 8 planes each.
+inline int plane_chunk(const heat_geom &g, int tile_x, int tile_y, long want = 152L * 16) {
+  const long tiles =
+      (long)((g.nx - 2 + tile_x - 1) / tile_x) * ((g.ny - 2 + tile_y - 1) / tile_y);
+  const long chunks = (want + tiles - 1) / tiles;
+  const int interior = g.nz - 2;
+  int kc = (int)((interior + chunks - 1) / chunks);
+  if (kc < 8) kc = 8;
+  if (kc > interior) kc = interior;
+  return kc;
+}
+
 // heat_fp64_exact.cu (compiled with --fmad=false)
 cudaError_t launch_exact_raw(double *u_new, const double *u_old, const double *rhs,
                              const double *kappa, const heat_geom &g, double factor,

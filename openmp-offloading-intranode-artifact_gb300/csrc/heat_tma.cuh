@@ -1,5 +1,5 @@
-// TMA plane-tile loads and mbarrier waits shared by the staged kernels
-// (heat_fp32c_tma.cu, heat_fp64_stage.cu).
+// TMA plane-tile loads and mbarrier waits for kernels that stage plane tiles
+// in shared memory (heat_fp32c_tma.cu).
 //
 // A block's thread 0 issues cp.async.bulk.tensor 3-D box loads of plane tiles
 // into a shared-memory ring; each ring slot completes on its own mbarrier
@@ -90,7 +90,9 @@ inline EncodeTiledFn encoder() {
   static EncodeTiledFn fn = [] {
     void *p = nullptr;
     cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) !=
+    // the entry point as the CUDA 12.0 driver API defines it
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) !=
             cudaSuccess ||
         q != cudaDriverEntryPointSuccess) {
       cudaGetLastError();
