@@ -58,12 +58,12 @@ def test_golden_inputs_are_the_reference_expressions(oracle):
         assert h == z["meta"][2] and dt == z["meta"][3]
 
 
-@pytest.mark.skipif(not Path("/root/reference/OpenMP_Single_Source/heat3D_variable_coeff.c").exists(),
-                    reason="reference source tree not present on this machine")
 @pytest.mark.parametrize("n,steps", [(9, 7), (20, 13), (33, 11)])
 def test_oracle_cli_equals_reference_serial(oracle, n, steps):
     """heat_ref N T prints the same step count and writes the same dump as serial."""
     oracle.build()
+    if not oracle.REF_SERIAL.exists():
+        pytest.skip("the reference serial is built only where the reference source tree is present")
     T = "%.17g" % oracle.verify_T(n, steps)
     with tempfile.TemporaryDirectory() as td:
         env = {**os.environ, "WRITE_TXT": "1", "OMP_NUM_THREADS": "4"}
