@@ -178,14 +178,16 @@ int heat_tune_lookup(int precision, unsigned flags, int nz, int *kchunk);
 
 /* ---- continuous-batching solve server ------------------------------------ */
 
-/* No counterpart in the reference.  A server owns one GPU worker thread and
- * `prep_threads` input-generation threads.  Submitted requests get seeded
- * synthetic inputs (heat_inputs_config), are admitted in arrival order while
- * their device bytes fit `budget_bytes` (a request that does not fit waits;
- * the next few behind it may go first), stay device-resident until done, and
- * advance together through a heat_batch in ticks of `tick_steps` steps; new
- * requests join at the next tick as memory frees up.  A request larger than
- * the whole budget completes with status HEAT_EBUDGET.                       */
+/* No counterpart in the reference.  A server owns one GPU worker thread, two
+ * context-creation threads and `prep_threads` input-generation threads.
+ * Submitted requests get seeded synthetic inputs (heat_inputs_config, into
+ * pinned host buffers the server reuses; at most 16 GB ahead of admission),
+ * are admitted in arrival order while their device bytes fit `budget_bytes`
+ * (a request that does not fit waits; the next few behind it may go first),
+ * stay device-resident until done, and advance together through a heat_batch
+ * in ticks of `tick_steps` steps; new requests join at the next tick as memory
+ * frees up.  A request larger than the whole budget completes with status
+ * HEAT_EBUDGET.                                                              */
 typedef struct heat_server heat_server;
 
 typedef struct heat_request {
