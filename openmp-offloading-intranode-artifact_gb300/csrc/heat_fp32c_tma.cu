@@ -11,8 +11,11 @@
 //   1. computes step t+1 on plane k+1 over the tile plus a 1-point halo
 //      (34 x 18 points) from ring planes k, k+1, k+2 into a 3-plane ring of
 //      intermediate values, and
-//   2. computes step t+2 on plane k over the tile from intermediate planes
-//      k-1, k, k+1 and writes it to global memory.
+//   2. computes step t+2 on plane k-1 over the tile from intermediate planes
+//      k-2, k-1, k and writes it to global memory.
+// Running step t+2 one plane behind step t+1 leaves one block barrier per
+// plane (it publishes the landed input plane and the previous iteration's
+// intermediate plane together); at 48 registers two blocks fit on an SM.
 // Global traffic per two updates: the five input arrays read once (plus the
 // halo, mostly served by L2) and v, carry written once -- about half of two
 // single steps.  The per-point arithmetic is exactly the single-step column
@@ -72,7 +75,7 @@ struct Maps {
   CUtensorMap v, c, wx, wy, wz;
 };
 
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, 2)
     k_fp32c_tb2(const __grid_constant__ Maps in, float *__restrict__ vn,
                 uint16_t *__restrict__ cn, int nx, int ny, int nz, int P, size_t S, int kchunk,
                 int *__restrict__ err) {
@@ -181,37 +184,32 @@ __global__ void __launch_bounds__(NT, 3)
   wait_plane(kb);
   wait_plane(kb + 1);
   failed = __syncthreads_or(failed);
-  float vm = 0.f, v0 = 0.f, wzm = 0.f;    // level-1 window: v(p-1), v(p), wz(p-1)
-  float l1m = 0.f, l1c = 0.f, c1c = 0.f;  // own step-(t+1) values at k-1, k; carry at k
-  float wz2m = 0.f;                       // wz at plane k-1 (for step t+2 at k)
-  W wc{};                                 // weights at plane k (for step t+2 at k)
+  // Level-1 window: v(p-1), v(p), wz(p-1) for the next plane p to compute.
+  float vm = 0.f, v0 = 0.f, wzm = 0.f;
+  // Level-2 window at the top of iteration k: own step-(t+1) values at planes
+  // k-2, k-1, k, the carries at k-1, k, the weights at k-1, k and wz at k-2.
+  float l1a = 0.f, l1b = 0.f, l1cc = 0.f;
+  float c1b = 0.f, c1cc = 0.f;
+  W wb{}, wcc{};
+  float wza = 0.f;
   if (!failed && l1_ok) {
     if (kb - 2 >= 0) {
       vm = sm.ring[(kb - 2) % R].v[o];
       wzm = sm.ring[(kb - 2) % R].wz[o];
     }
     v0 = sm.ring[(kb - 1) % R].v[o];
-    W wa;
-    float ta, ca;
     float vp = sm.ring[kb % R].v[o];
-    level1(kb - 1, vm, v0, vp, wzm, wa, ta, ca);
-    sm.v1[(kb - 1) % 3][tid] = ta;
-    vm = v0;
-    v0 = vp;
-    wzm = wa.z;
-    W wb;
-    float tb, cb;
-    vp = sm.ring[(kb + 1) % R].v[o];
-    level1(kb, vm, v0, vp, wzm, wb, tb, cb);
-    sm.v1[kb % 3][tid] = tb;
+    level1(kb - 1, vm, v0, vp, wzm, wb, l1b, c1b);
+    sm.v1[(kb - 1) % 3][tid] = l1b;
     vm = v0;
     v0 = vp;
     wzm = wb.z;
-    l1m = ta;
-    l1c = tb;
-    c1c = cb;
-    wz2m = wa.z;
-    wc = wb;
+    vp = sm.ring[(kb + 1) % R].v[o];
+    level1(kb, vm, v0, vp, wzm, wcc, l1cc, c1cc);
+    sm.v1[kb % 3][tid] = l1cc;
+    vm = v0;
+    v0 = vp;
+    wzm = wcc.z;
   }
   // The prologue's reads of planes kb-2 and kb-1 are done: their slots take
   // planes kb+2 and kb+3.
@@ -221,19 +219,20 @@ __global__ void __launch_bounds__(NT, 3)
     issue(kb + 3);
   }
 
-  size_t g = (size_t)kb * S + (size_t)gy * P + gx;
-  for (int k = kb; k < ke && !failed; ++k, g += S) {
+  // Step t+2 runs one plane behind step t+1: iteration k computes step t+1 on
+  // plane k+1 and step t+2 on plane k-1, so the one barrier at the top of an
+  // iteration publishes both the landed plane k+2 and the previous
+  // iteration's step-(t+1) plane k, and retires ring slot k % R and
+  // intermediate slot (k+1) % 3 for reuse.  Iteration kb writes no output
+  // (plane kb-1 is outside the chunk); iteration ke computes no step t+1.
+  for (int k = kb; k <= ke && !failed; ++k) {
     wait_plane(k + 2);
-    // One barrier both publishes plane k+2 and retires iteration k-1: plane
-    // k's ring slot (read last by level 1 of plane k) and intermediate slot
-    // (k+1) % 3 are free after it.  Weights of planes k and k-1 live in
-    // registers, so only planes k+1 and k+2 stay resident.
     failed = __syncthreads_or(failed);
     if (failed) break;
     issue(k + 4);
     W wn{};
     float l1p = 0.f, c1p = 0.f;
-    if (l1_ok) {
+    if (k + 1 <= ke && l1_ok) {
       const float vp = sm.ring[(k + 2) % R].v[o];
       level1(k + 1, vm, v0, vp, wzm, wn, l1p, c1p);
       sm.v1[(k + 1) % 3][tid] = l1p;
@@ -241,27 +240,30 @@ __global__ void __launch_bounds__(NT, 3)
       v0 = vp;
       wzm = wn.z;
     }
-    __syncthreads();
-    if (out_ok) {
-      const float *vk = sm.v1[k % 3];
+    if (k - 1 >= kb && out_ok) {
+      const float *vk = sm.v1[(k - 1) % 3];
       float d = 0.0f;
-      d = fmaf(wc.x, vk[tid + 1] - l1c, d);
-      d = fmaf(wc.xm, vk[tid - 1] - l1c, d);
-      d = fmaf(wc.y, vk[tid + L1X] - l1c, d);
-      d = fmaf(wc.ym, vk[tid - L1X] - l1c, d);
-      d = fmaf(wc.z, l1p - l1c, d);
-      d = fmaf(wz2m, l1m - l1c, d);
-      const float yk = __fsub_rn(d, c1c);
-      const float t = __fadd_rn(l1c, yk);
-      const float cc = __fsub_rn(__fsub_rn(t, l1c), yk);
+      d = fmaf(wb.x, vk[tid + 1] - l1b, d);
+      d = fmaf(wb.xm, vk[tid - 1] - l1b, d);
+      d = fmaf(wb.y, vk[tid + L1X] - l1b, d);
+      d = fmaf(wb.ym, vk[tid - L1X] - l1b, d);
+      d = fmaf(wb.z, l1cc - l1b, d);
+      d = fmaf(wza, l1a - l1b, d);
+      const float yk = __fsub_rn(d, c1b);
+      const float t = __fadd_rn(l1b, yk);
+      const float cc = __fsub_rn(__fsub_rn(t, l1b), yk);
+      const size_t g = (size_t)(k - 1) * S + (size_t)gy * P + gx;
       vn[g] = t;
       cn[g] = walk::f2bf(cc);
     }
-    l1m = l1c;
-    l1c = l1p;
-    c1c = c1p;
-    wz2m = wc.z;
-    wc = wn;
+    l1a = l1b;
+    l1b = l1cc;
+    l1cc = l1p;
+    c1b = c1cc;
+    c1cc = c1p;
+    wza = wb.z;
+    wb = wcc;
+    wcc = wn;
   }
   if (failed) {
     if (tid == 0) atomicExch(err, 1);
@@ -295,10 +297,8 @@ cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, cons
   if (!encode(&m.v, v, false, g) || !encode(&m.c, cr, true, g) || !encode(&m.wx, w[0], false, g) ||
       !encode(&m.wy, w[1], false, g) || !encode(&m.wz, w[2], false, g))
     return cudaErrorInvalidValue;
-  static bool attr = [] {
-    return cudaFuncSetAttribute(k_fp32c_tb2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)fp32c_tb2_smem()) == cudaSuccess;
-  }();
+  static bool attr = cudaFuncSetAttribute(k_fp32c_tb2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)fp32c_tb2_smem()) == cudaSuccess;
   if (!attr) return cudaErrorInvalidConfiguration;
   const int bx = (g.nx - 2 + OX - 1) / OX, by = (g.ny - 2 + OY - 1) / OY;
   const int interior = g.nz - 2;
