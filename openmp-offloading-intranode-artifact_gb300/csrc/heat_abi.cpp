@@ -101,8 +101,13 @@ int dalloc(T **p, size_t count, cudaStream_t st) {
   return HEAT_OK;
 }
 
-// Copy a dense host k-j-i array into the pitched device layout.
+// Copy a dense host k-j-i array into the pitched device layout (one
+// contiguous copy when the rows carry no padding).
 int upload(double *dst, const double *src, const heat_geom &g, cudaStream_t st) {
+  if (g.pitch == g.nx) {
+    CK(cudaMemcpyAsync(dst, src, g.elems * sizeof(double), cudaMemcpyHostToDevice, st));
+    return HEAT_OK;
+  }
   CK(cudaMemcpy2DAsync(dst, (size_t)g.pitch * sizeof(double), src, (size_t)g.nx * sizeof(double),
                        (size_t)g.nx * sizeof(double), (size_t)g.ny * g.nz,
                        cudaMemcpyHostToDevice, st));
@@ -110,6 +115,10 @@ int upload(double *dst, const double *src, const heat_geom &g, cudaStream_t st) 
 }
 
 int download(double *dst, const double *src, const heat_geom &g, cudaStream_t st) {
+  if (g.pitch == g.nx) {
+    CK(cudaMemcpyAsync(dst, src, g.elems * sizeof(double), cudaMemcpyDeviceToHost, st));
+    return HEAT_OK;
+  }
   CK(cudaMemcpy2DAsync(dst, (size_t)g.nx * sizeof(double), src, (size_t)g.pitch * sizeof(double),
                        (size_t)g.nx * sizeof(double), (size_t)g.ny * g.nz,
                        cudaMemcpyDeviceToHost, st));
@@ -196,11 +205,54 @@ int load_split(heat_ctx *c, double *tmp, const double *u_host) {
   return HEAT_OK;
 }
 
+// A second stream for a context's set-up: work enqueued on it starts after
+// everything already on the context's stream, and join() makes the context's
+// stream wait for it.  Released (after its work completes) on every return.
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t ev = nullptr;
+
+  bool begin(cudaStream_t main) {
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventRecord(ev, main) != cudaSuccess || cudaStreamWaitEvent(s, ev, 0) != cudaSuccess) {
+      cudaGetLastError();
+      release();
+      return false;
+    }
+    return true;
+  }
+  cudaError_t join(cudaStream_t main) {
+    cudaError_t e = cudaEventRecord(ev, s);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(main, ev, 0);
+    return e;
+  }
+  void release() {
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+      s = nullptr;
+    }
+    if (ev) {
+      cudaEventDestroy(ev);
+      ev = nullptr;
+    }
+  }
+  ~SideStream() { release(); }
+};
+
+// Fields of at least this many bytes upload u0 on a side stream, overlapping
+// the kappa upload and the weight set-up kernels.
+constexpr size_t kSideUploadBytes = 64u << 20;
+
 int init_fp64(heat_ctx *c, const heat_desc *d) {
   const heat_geom &g = c->g;
   const size_t bytes = g.elems * sizeof(double);
   int rc = HEAT_OK;
   double *kap = nullptr;  // raw kappa on the device (kept only for the naive kernel)
+  SideStream side;
+  bool split = false;
+  cudaStream_t ust = c->stream;  // stream of the u0 upload
 #define TRY(x)                    \
   do {                            \
     rc = (x);                     \
@@ -219,23 +271,24 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemset");
     goto done;
   }
-  TRY(upload(c->u[0], d->u0, g, c->stream));
+  // kappa first: the weight set-up kernels need it, and u0 (and the source
+  // term) then upload on the side stream while they run.
+  if (d->rhs) TRY(dalloc(&c->rhs, g.elems, c->stream));
+  if (d->rhs && g.pitch != g.nx && cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "cudaMemset");
+    goto done;
+  }
   TRY(upload(kap, d->kappa, g, c->stream));
+  split = bytes >= kSideUploadBytes && side.begin(c->stream);
+  if (split) ust = side.s;
+  TRY(upload(c->u[0], d->u0, g, ust));
   // u_new starts as a copy of u0, so its boundary holds the same values
   // (the reference seeds both buffers from u0, 1-cuda.cu:219-222).
-  if (cudaMemcpyAsync(c->u[1], c->u[0], bytes, cudaMemcpyDeviceToDevice, c->stream) !=
-      cudaSuccess) {
+  if (cudaMemcpyAsync(c->u[1], c->u[0], bytes, cudaMemcpyDeviceToDevice, ust) != cudaSuccess) {
     rc = cuda_fail(cudaGetLastError(), "cudaMemcpy u0");
     goto done;
   }
-  if (d->rhs) {
-    TRY(dalloc(&c->rhs, g.elems, c->stream));
-    if (g.pitch != g.nx && cudaMemsetAsync(c->rhs, 0, bytes, c->stream) != cudaSuccess) {
-      rc = cuda_fail(cudaGetLastError(), "cudaMemset");
-      goto done;
-    }
-    TRY(upload(c->rhs, d->rhs, g, c->stream));
-  }
+  if (d->rhs) TRY(upload(c->rhs, d->rhs, g, ust));
   if (c->flags & HEAT_NAIVE) {
     c->kappa = kap;
     kap = nullptr;
@@ -281,9 +334,14 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
       c->launches += 1;
     }
   }
+  if (split && side.join(c->stream) != cudaSuccess) {
+    rc = cuda_fail(cudaGetLastError(), "u0 upload join");
+    goto done;
+  }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess)
     rc = cuda_fail(cudaGetLastError(), "heat_init sync");
 done:
+  side.release();
   if (kap) cudaFreeAsync(kap, c->stream);
   return rc;
 #undef TRY
