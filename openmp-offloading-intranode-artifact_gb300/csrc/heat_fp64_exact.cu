@@ -15,8 +15,6 @@
 // face (IEEE addition is commutative), so the z-march below carries E of
 // plane k as F of plane k+1 and stays bit-identical.
 
-#include <cstdlib>
-
 #include "heat_internal.h"
 #include "heat_walk.cuh"
 
@@ -47,66 +45,103 @@ __global__ void k_naive(double *__restrict__ un, const double *__restrict__ u,
   un[c] = combine(RHS ? __dadd_rn(uc, rhs[c]) : uc, factor, A, B, C, D, E, F);
 }
 
-// z-marching kernels: a (32 x 8) thread tile of (i, j) columns walks a chunk
-// of planes; the lower flux and the two z-neighbours stay in registers.
-constexpr int TX = 32, TY = 8;
-
-// z-marching kernel: a (32 x 8) thread tile of columns walks a chunk of
-// planes; the lower flux and the z-neighbours stay in registers.  The west
-// face flux comes from the neighbouring lane: B at column i is the value A of
-// column i-1 (same operands, same order), so each point computes one x-flux
-// instead of two.  A warp covers 31 output columns; its lane 0 walks the
-// column west of them only to hand over its A.  Lanes past the grid's
-// interior walk the last interior column (in-bounds loads) and store nothing.
+// z-marching kernel.  A (32 x 8) thread tile walks a chunk of planes; each
+// thread owns one column i of RY adjacent rows, and the lower flux and the
+// z-neighbours of each row stay in registers.  Two face fluxes are shared
+// instead of recomputed (a face flux is the same rounded value seen from both
+// cells that share the face):
+//   - x: B at column i is A of column i-1 (same operands, same order), taken
+//     from the neighbouring lane.  A warp covers 31 output columns; its lane 0
+//     walks the column west of them only to hand over its A.  Lanes past the
+//     grid's interior walk the last interior column (in-bounds loads) and
+//     store nothing.
+//   - y: C of row j is D of row j+1, so a thread computes RY+1 y-fluxes for
+//     its RY outputs instead of 2 RY.  Row t of a thread (t = 0 .. RY+1) is
+//     grid row j0-1+t; rows past the grid are clamped to the last row so every
+//     load stays in bounds, and only interior rows store (an interior row reads
+//     rows j-1, j, j+1 only, none of them clamped).
 // RAW forms the face kappa sums from kappa as the reference does each step
 // (the drop-in heat_update); otherwise they are read precomputed, once per
 // context: kx[c] = kappa[c] + kappa[c+1], ky[c] = kappa[c] + kappa[c+P],
-// kz[c] = kappa[c] + kappa[c+S] -- the same values, 3 additions per point fewer.
+// kz[c] = kappa[c] + kappa[c+S] -- the same values, fewer additions per point.
+// Three rows per thread measured best at 512^3 (GLUP/s, drop-in / context
+// form): one row 24.0 / 31.9, two 26.4 / 34.6, three 26.7 / 35.1, four
+// 26.3 / 34.5 (123 registers).
+constexpr int TX = 32, TY = 8;
 constexpr int SX = 31;
+constexpr int RY = 3;
 
 template <bool RHS, bool RAW>
 __global__ void __launch_bounds__(TX *TY)
-    k_exact_shfl(double *__restrict__ un, const double *__restrict__ u,
+    k_exact_rows(double *__restrict__ un, const double *__restrict__ u,
                  const double *__restrict__ rhs, const double *__restrict__ kap,
                  const double *__restrict__ kx, const double *__restrict__ ky,
                  const double *__restrict__ kz, int nx, int ny, int nz, int P, size_t S,
                  double factor, int kchunk) {
   const int lane = threadIdx.x;
   const int i = blockIdx.x * SX + lane;  // lane 0: the column west of the outputs
-  const int j = 1 + blockIdx.y * TY + threadIdx.y;
+  const int j0 = 1 + (blockIdx.y * TY + threadIdx.y) * RY;
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
-  if (j >= ny - 1 || kb >= ke) return;  // uniform across the warp
-  const bool store = lane >= 1 && i <= nx - 2;
+  if (j0 >= ny - 1 || kb >= ke) return;  // uniform across the warp
+  const bool xs = lane >= 1 && i <= nx - 2;
   const int ic = min(i, nx - 2);
-  size_t c = (size_t)kb * S + (size_t)j * P + ic;
-  double uc = u[c];
-  double kc = RAW ? kap[c] : 0.0;
-  double F = RAW ? flux(__dadd_rn(kc, kap[c - S]), uc, u[c - S]) : flux(kz[c - S], uc, u[c - S]);
-  for (int k = kb; k < ke; ++k, c += S) {
-    const double uu = u[c + S];
-    const double ku = RAW ? kap[c + S] : 0.0;
-    const double A = RAW ? flux(__dadd_rn(kap[c + 1], kc), u[c + 1], uc)
-                         : flux(kx[c], u[c + 1], uc);
-    const double B = __shfl_up_sync(0xffffffffu, A, 1);
-    const double C = RAW ? flux(__dadd_rn(kap[c + P], kc), u[c + P], uc)
-                         : flux(ky[c], u[c + P], uc);
-    const double D = RAW ? flux(__dadd_rn(kc, kap[c - P]), uc, u[c - P])
-                         : flux(ky[c - P], uc, u[c - P]);
-    const double E = RAW ? flux(__dadd_rn(ku, kc), uu, uc) : flux(kz[c], uu, uc);
-    if (store) un[c] = combine(RHS ? __dadd_rn(uc, rhs[c]) : uc, factor, A, B, C, D, E, F);
-    F = E;
-    uc = uu;
-    kc = ku;
+  size_t ro[RY + 2];
+#pragma unroll
+  for (int t = 0; t < RY + 2; ++t) ro[t] = (size_t)min(j0 - 1 + t, ny - 1) * P + ic;
+  size_t pl = (size_t)kb * S;
+  double uc[RY + 2], kc[RY + 2], F[RY];
+#pragma unroll
+  for (int t = 0; t < RY + 2; ++t) {
+    uc[t] = u[pl + ro[t]];
+    kc[t] = RAW ? kap[pl + ro[t]] : 0.0;
+  }
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    const size_t q = pl - S + ro[r + 1];
+    F[r] = RAW ? flux(__dadd_rn(kc[r + 1], kap[q]), uc[r + 1], u[q])
+               : flux(kz[q], uc[r + 1], u[q]);
+  }
+  for (int k = kb; k < ke; ++k, pl += S) {
+    double uu[RY + 2], ku[RY + 2], G[RY + 1];
+#pragma unroll
+    for (int t = 0; t < RY + 2; ++t) {
+      uu[t] = u[pl + S + ro[t]];
+      ku[t] = RAW ? kap[pl + S + ro[t]] : 0.0;
+    }
+    // G[t]: the flux through the face between rows t and t+1
+#pragma unroll
+    for (int t = 0; t <= RY; ++t)
+      G[t] = RAW ? flux(__dadd_rn(kc[t + 1], kc[t]), uc[t + 1], uc[t])
+                 : flux(ky[pl + ro[t]], uc[t + 1], uc[t]);
+#pragma unroll
+    for (int r = 0; r < RY; ++r) {
+      const int t = r + 1;
+      const size_t q = pl + ro[t];
+      const double A = RAW ? flux(__dadd_rn(kap[q + 1], kc[t]), u[q + 1], uc[t])
+                           : flux(kx[q], u[q + 1], uc[t]);
+      const double B = __shfl_up_sync(0xffffffffu, A, 1);
+      const double E = RAW ? flux(__dadd_rn(ku[t], kc[t]), uu[t], uc[t]) : flux(kz[q], uu[t], uc[t]);
+      if (xs && j0 + r <= ny - 2)
+        un[q] = combine(RHS ? __dadd_rn(uc[t], rhs[q]) : uc[t], factor, A, B, G[t], G[t - 1], E,
+                        F[r]);
+      F[r] = E;
+    }
+#pragma unroll
+    for (int t = 0; t < RY + 2; ++t) {
+      uc[t] = uu[t];
+      kc[t] = ku[t];
+    }
   }
 }
 
 template <bool RHS, bool RAW>
-void launch_shfl(double *u_new, const double *u_old, const double *rhs, const double *kappa,
+void launch_rows(double *u_new, const double *u_old, const double *rhs, const double *kappa,
                  double *const ks[3], const heat_geom &g, double factor, cudaStream_t st) {
-  const int kc = plane_chunk(g, SX, TY);
-  dim3 gr((g.nx - 2 + SX - 1) / SX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
-  k_exact_shfl<RHS, RAW><<<gr, dim3(TX, TY), 0, st>>>(
+  const int kc = plane_chunk(g, SX, TY * RY);
+  dim3 gr((g.nx - 2 + SX - 1) / SX, (g.ny - 2 + TY * RY - 1) / (TY * RY),
+          (g.nz - 2 + kc - 1) / kc);
+  k_exact_rows<RHS, RAW><<<gr, dim3(TX, TY), 0, st>>>(
       u_new, u_old, rhs, kappa, ks ? ks[0] : nullptr, ks ? ks[1] : nullptr,
       ks ? ks[2] : nullptr, g.nx, g.ny, g.nz, g.pitch, g.plane, factor, kc);
 }
@@ -146,22 +181,20 @@ cudaError_t launch_naive(double *u_new, const double *u_old, const double *rhs,
 cudaError_t launch_exact_raw(double *u_new, const double *u_old, const double *rhs,
                              const double *kappa, const heat_geom &g, double factor,
                              cudaStream_t st) {
-  // the lane-shuffled walk: 23.9 GLUP/s at 512^3 against 21.9 for k_exact_raw
   if (rhs)
-    launch_shfl<true, true>(u_new, u_old, rhs, kappa, nullptr, g, factor, st);
+    launch_rows<true, true>(u_new, u_old, rhs, kappa, nullptr, g, factor, st);
   else
-    launch_shfl<false, true>(u_new, u_old, rhs, kappa, nullptr, g, factor, st);
+    launch_rows<false, true>(u_new, u_old, rhs, kappa, nullptr, g, factor, st);
   return cudaGetLastError();
 }
 
 cudaError_t launch_exact_faces(double *u_new, const double *u_old, const double *rhs,
                                double *const ks[3], const heat_geom &g, double factor,
                                cudaStream_t st) {
-  // the lane-shuffled walk: 31.9 GLUP/s at 512^3 against 29.7 for k_exact_faces
   if (rhs)
-    launch_shfl<true, false>(u_new, u_old, rhs, nullptr, ks, g, factor, st);
+    launch_rows<true, false>(u_new, u_old, rhs, nullptr, ks, g, factor, st);
   else
-    launch_shfl<false, false>(u_new, u_old, rhs, nullptr, ks, g, factor, st);
+    launch_rows<false, false>(u_new, u_old, rhs, nullptr, ks, g, factor, st);
   return cudaGetLastError();
 }
 
