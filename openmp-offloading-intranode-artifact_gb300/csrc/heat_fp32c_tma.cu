@@ -38,7 +38,7 @@ namespace heat {
 namespace {
 
 constexpr int OX = 32, OY = 16;          // output tile
-constexpr int BXF = 40, BXC = 48, BY = 20;  // TMA boxes (float arrays, BF16 carry)
+constexpr int BXF = 40, BXC = 48, BY = OY + 4;  // TMA boxes (float arrays, BF16 carry)
 constexpr int L1X = OX + 2, L1Y = OY + 2;   // step-(t+1) region
 constexpr int NT = ((L1X * L1Y + 31) / 32) * 32;  // one thread per step-(t+1) point
 constexpr int R = 4;                     // ring depth (planes)
@@ -46,14 +46,22 @@ constexpr int R = 4;                     // ring depth (planes)
 constexpr int kPlaneF = BXF * BY;        // floats per float-array plane tile
 constexpr int kPlaneC = BXC * BY;        // BF16 per carry plane tile
 constexpr unsigned kSlotBytes = 4u * kPlaneF * 4u + 2u * kPlaneC;  // v, wx, wy, wz + carry
+// A TMA tile copy writes shared memory from a 128-byte aligned address, so
+// each array of a slot starts on a 128-byte boundary: arrays are strided by
+// their box size rounded up to 128 bytes (the copies still move box bytes).
+constexpr int kStrideF = (kPlaneF * 4 + 127) / 128 * 128 / 4;
+constexpr int kStrideC = (kPlaneC * 2 + 127) / 128 * 128 / 2;
+static_assert((kStrideF * 4) % 128 == 0 && (kStrideC * 2) % 128 == 0,
+              "slot arrays must start on 128-byte boundaries");
 
 struct __align__(128) Slot {
-  float v[kPlaneF];
-  float wx[kPlaneF];
-  float wy[kPlaneF];
-  float wz[kPlaneF];
-  uint16_t c[kPlaneC];
+  float v[kStrideF];
+  float wx[kStrideF];
+  float wy[kStrideF];
+  float wz[kStrideF];
+  uint16_t c[kStrideC];
 };
+static_assert(sizeof(Slot) % 128 == 0, "ring slots must start on 128-byte boundaries");
 
 struct Smem {
   Slot ring[R];
