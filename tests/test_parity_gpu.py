@@ -80,6 +80,21 @@ def test_reference_problem_larger(H, oracle, case):
         assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, (fl, m)
 
 
+def test_large_padded_field_with_source_term(H, oracle):
+    """A field of >= 64 MiB with padded rows (n = 259, row pitch 260) and a
+    source term: heat_init uploads u0 and rhs on a side stream while the
+    weight set-up kernels run, and zeroes the padding columns first."""
+    n, steps = 259, 3
+    kappa, rhs, u0, h, dt = H.inputs_reference(n)
+    u_or = oracle.steps(u0, kappa, h, dt, steps, rhs=rhs)
+    u_ex, _, _ = solve(H, kappa, u0, h, dt, steps=steps, rhs=rhs, flags=1)
+    assert bits_equal(u_ex, u_or)
+    for fl in FAST:
+        u_fa, _, _ = solve(H, kappa, u0, h, dt, steps=steps, rhs=rhs, flags=fl)
+        m = metrics(u_or, u_fa)
+        assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, (fl, m)
+
+
 SHAPES = [(3, 3, 3), (4, 5, 6), (5, 4, 3), (33, 17, 9), (31, 33, 35), (64, 8, 40), (130, 67, 21)]
 
 
