@@ -42,6 +42,7 @@ constexpr int BXF = 40, BXC = 48, BY = OY + 4;  // TMA boxes (float arrays, BF16
 constexpr int L1X = OX + 2, L1Y = OY + 2;   // step-(t+1) region
 constexpr int NT = ((L1X * L1Y + 31) / 32) * 32;  // one thread per step-(t+1) point
 constexpr int R = 4;                     // ring depth (planes)
+static_assert((R & (R - 1)) == 0, "slot index p & (R - 1) needs R a power of two");
 
 constexpr int kPlaneF = BXF * BY;        // floats per float-array plane tile
 constexpr int kPlaneC = BXC * BY;        // BF16 per carry plane tile
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(NT, 2)
   const bool waiter = tid < 32;
   auto issue = [&](int p) {
     if (p < pmin || p > pmax) return;
-    const int s = p % R;
+    const int s = p & (R - 1);
     pending |= 1u << s;
     if (tid != 0) return;
     Slot &sl = sm.ring[s];
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(NT, 2)
   };
   auto wait_plane = [&](int p) {
     if (p < pmin || p > pmax || failed) return;
-    const int s = p % R;
+    const int s = p & (R - 1);
     if (waiter && !mbar_wait(&sm.bar[s], (phase >> s) & 1u)) {
       failed = true;
       return;
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(NT, 2)
   // and the plane's weights.
   auto level1 = [&](int p, float vm, float v0, float vp, float wzm, W &wp, float &t1,
                     float &c1) {
-    const Slot &cur = sm.ring[p % R];
+    const Slot &cur = sm.ring[p & (R - 1)];
     wp.x = cur.wx[o];
     wp.xm = cur.wx[o - 1];
     wp.y = cur.wy[o];
@@ -202,17 +203,17 @@ __global__ void __launch_bounds__(NT, 2)
   float wza = 0.f;
   if (!failed && l1_ok) {
     if (kb - 2 >= 0) {
-      vm = sm.ring[(kb - 2) % R].v[o];
-      wzm = sm.ring[(kb - 2) % R].wz[o];
+      vm = sm.ring[(kb - 2) & (R - 1)].v[o];
+      wzm = sm.ring[(kb - 2) & (R - 1)].wz[o];
     }
-    v0 = sm.ring[(kb - 1) % R].v[o];
-    float vp = sm.ring[kb % R].v[o];
+    v0 = sm.ring[(kb - 1) & (R - 1)].v[o];
+    float vp = sm.ring[kb & (R - 1)].v[o];
     level1(kb - 1, vm, v0, vp, wzm, wb, l1b, c1b);
     sm.v1[(kb - 1) % 3][tid] = l1b;
     vm = v0;
     v0 = vp;
     wzm = wb.z;
-    vp = sm.ring[(kb + 1) % R].v[o];
+    vp = sm.ring[(kb + 1) & (R - 1)].v[o];
     level1(kb, vm, v0, vp, wzm, wcc, l1cc, c1cc);
     sm.v1[kb % 3][tid] = l1cc;
     vm = v0;
@@ -230,10 +231,14 @@ __global__ void __launch_bounds__(NT, 2)
   // Step t+2 runs one plane behind step t+1: iteration k computes step t+1 on
   // plane k+1 and step t+2 on plane k-1, so the one barrier at the top of an
   // iteration publishes both the landed plane k+2 and the previous
-  // iteration's step-(t+1) plane k, and retires ring slot k % R and
-  // intermediate slot (k+1) % 3 for reuse.  Iteration kb writes no output
+  // iteration's step-(t+1) plane k, and retires ring slot k mod R and
+  // intermediate slot (k+1) mod 3 for reuse.  Iteration kb writes no output
   // (plane kb-1 is outside the chunk); iteration ke computes no step t+1.
-  for (int k = kb; k <= ke && !failed; ++k) {
+  // Intermediate slots of planes k-1, k, k+1 and the output offset of plane
+  // k-1, advanced with k.
+  int ia = (kb + 2) % 3, ib = kb % 3, ic = (kb + 1) % 3;
+  size_t g = (size_t)(kb - 1) * S + (size_t)gy * P + gx;
+  for (int k = kb; k <= ke && !failed; ++k, g += S) {
     wait_plane(k + 2);
     failed = __syncthreads_or(failed);
     if (failed) break;
@@ -241,15 +246,15 @@ __global__ void __launch_bounds__(NT, 2)
     W wn{};
     float l1p = 0.f, c1p = 0.f;
     if (k + 1 <= ke && l1_ok) {
-      const float vp = sm.ring[(k + 2) % R].v[o];
+      const float vp = sm.ring[(k + 2) & (R - 1)].v[o];
       level1(k + 1, vm, v0, vp, wzm, wn, l1p, c1p);
-      sm.v1[(k + 1) % 3][tid] = l1p;
+      sm.v1[ic][tid] = l1p;
       vm = v0;
       v0 = vp;
       wzm = wn.z;
     }
     if (k - 1 >= kb && out_ok) {
-      const float *vk = sm.v1[(k - 1) % 3];
+      const float *vk = sm.v1[ia];
       float d = 0.0f;
       d = fmaf(wb.x, vk[tid + 1] - l1b, d);
       d = fmaf(wb.xm, vk[tid - 1] - l1b, d);
@@ -260,7 +265,6 @@ __global__ void __launch_bounds__(NT, 2)
       const float yk = __fsub_rn(d, c1b);
       const float t = __fadd_rn(l1b, yk);
       const float cc = __fsub_rn(__fsub_rn(t, l1b), yk);
-      const size_t g = (size_t)(k - 1) * S + (size_t)gy * P + gx;
       vn[g] = t;
       cn[g] = walk::f2bf(cc);
     }
@@ -272,6 +276,10 @@ __global__ void __launch_bounds__(NT, 2)
     wza = wb.z;
     wb = wcc;
     wcc = wn;
+    const int t3 = ia;
+    ia = ib;
+    ib = ic;
+    ic = t3;
   }
   if (failed) {
     if (tid == 0) atomicExch(err, 1);
