@@ -104,15 +104,15 @@ __global__ void __launch_bounds__(NT, 2)
   }
   __syncthreads();
 
-  // Every thread keeps the same bookkeeping (which slots have a load in
-  // flight, and each slot's next completion parity); thread 0 issues the TMA
-  // and warp 0 alone spins on the mbarrier -- the block barrier after the
-  // wait hands the landed tile to the other warps.
+  // Warp 0 keeps the bookkeeping (which slots have a load in flight, and each
+  // slot's next completion parity) and alone spins on the mbarrier; thread 0
+  // issues the TMA.  The block barrier after the wait hands the landed tile to
+  // the other warps, which skip all of it (a warp-uniform branch).
   unsigned pending = 0, phase = 0;
   bool failed = false;
   const bool waiter = tid < 32;
   auto issue = [&](int p) {
-    if (p < pmin || p > pmax) return;
+    if (!waiter || p < pmin || p > pmax) return;
     const int s = p & (R - 1);
     pending |= 1u << s;
     if (tid != 0) return;
@@ -127,9 +127,9 @@ __global__ void __launch_bounds__(NT, 2)
     tma_load3(sl.c, &in.c, X0c, Y0, p, b);
   };
   auto wait_plane = [&](int p) {
-    if (p < pmin || p > pmax || failed) return;
+    if (!waiter || p < pmin || p > pmax || failed) return;
     const int s = p & (R - 1);
-    if (waiter && !mbar_wait(&sm.bar[s], (phase >> s) & 1u)) {
+    if (!mbar_wait(&sm.bar[s], (phase >> s) & 1u)) {
       failed = true;
       return;
     }
