@@ -238,6 +238,10 @@ __global__ void __launch_bounds__(NT, 2)
   // k-1, advanced with k.
   int ia = (kb + 2) % 3, ib = kb % 3, ic = (kb + 1) % 3;
   size_t g = (size_t)(kb - 1) * S + (size_t)gy * P + gx;
+  // Unrolled by the intermediate ring's period (3): the slot indices and the
+  // shift of the carried values resolve to fixed registers in each copy
+  // (512^3: 325 GLUP/s unrolled by 3, 308 not unrolled, 286 by 2).
+#pragma unroll 3
   for (int k = kb; k <= ke && !failed; ++k, g += S) {
     wait_plane(k + 2);
     failed = __syncthreads_or(failed);
