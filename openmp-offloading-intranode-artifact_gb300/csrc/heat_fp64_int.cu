@@ -44,8 +44,9 @@ __global__ void __launch_bounds__(TX *TYB, MINB)
 // warps 4-7 the integer rows.  Each warpgroup starts with setmaxnreg at the
 // launch count (64): no registers move between them, but the instruction
 // bounds each region for ptxas's allocator, which then spills half as much
-// (76 B against 152 B without it).  Measured at 512^3: 111 GLUP/s against 99
-// for the same kernel without setmaxnreg and 102-105 for k_fast_mix at 3
+// (76 B against 152 B without it).  Measured at 512^3: 111 GLUP/s (114 since
+// the FP64 walk's loop is unrolled by 2) against 99 for the same kernel
+// without setmaxnreg and 102-105 for k_fast_mix at 3
 // blocks per SM; moving registers from the FP64 to the integer warpgroup
 // (56/72, 48/80) or 3 blocks per SM with any split measured 83-105.  The host
 // launches it only when the compiled register count is kWsRegs, since a

@@ -344,6 +344,10 @@ __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *_
                                         size_t c, int kb, int ke) {
   HwCol<RHS> col;
   col.start(u, rhs, c0, cx, cy, cz, P, S, c);
+  // Unrolled by 2, the prefetch registers alternate instead of being copied
+  // into the working ones each plane (default launch at 512^3: 114 GLUP/s
+  // against 111.5; by 3 or 4 no gain).
+#pragma unroll 2
   for (int k = kb; k < ke; ++k) col.step(un, u, rhs, c0, cx, cy, cz, P, S, k + 1 < ke);
 }
 
