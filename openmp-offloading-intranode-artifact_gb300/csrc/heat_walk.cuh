@@ -346,8 +346,9 @@ __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *_
   col.start(u, rhs, c0, cx, cy, cz, P, S, c);
   // Unrolled by 2, the prefetch registers alternate instead of being copied
   // into the working ones each plane (default launch at 512^3: 114 GLUP/s
-  // against 111.5; by 3 or 4 no gain).
-#pragma unroll 2
+  // against 111.5; by 3 or 4 no gain).  Not with a source term: that launch
+  // holds 80 registers a thread and gains nothing (94.4 against 94.7-95.2).
+#pragma unroll (RHS ? 1 : 2)
   for (int k = kb; k < ke; ++k) col.step(un, u, rhs, c0, cx, cy, cz, P, S, k + 1 < ke);
 }
 
