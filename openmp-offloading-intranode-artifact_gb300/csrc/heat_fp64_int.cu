@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256, MINB)
     const int ke = min(kb + kchunk, nz - 1);
     if (i >= nx - 1 || j >= ny - 1 || kb >= ke) return;
     const size_t c = (size_t)kb * S + (size_t)j * P + i;
-    walk::walk_hw<RHS>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
+    walk::walk_hw<RHS, RHS ? 1 : 2>(un, u, rhs, c0, cx, cy, cz, P, S, c, kb, ke);
   } else {
     asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;\n" ::"n"(REGS));
     const int i = 1 + blockIdx.x * TX + threadIdx.x;

@@ -333,8 +333,9 @@ struct HwCol {
   }
 };
 
-// The FP64-pipe walk over one (i, j) column, planes [kb, ke).
-template <bool RHS>
+// The FP64-pipe walk over one (i, j) column, planes [kb, ke); the plane loop
+// unrolled UNROLL times.
+template <bool RHS, int UNROLL = 1>
 __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *__restrict__ u,
                                         const double *__restrict__ rhs,
                                         const double *__restrict__ c0,
@@ -345,10 +346,10 @@ __device__ __forceinline__ void walk_hw(double *__restrict__ un, const double *_
   HwCol<RHS> col;
   col.start(u, rhs, c0, cx, cy, cz, P, S, c);
   // Unrolled by 2, the prefetch registers alternate instead of being copied
-  // into the working ones each plane (default launch at 512^3: 114 GLUP/s
-  // against 111.5; by 3 or 4 no gain).  Not with a source term: that launch
-  // holds 80 registers a thread and gains nothing (94.4 against 94.7-95.2).
-#pragma unroll (RHS ? 1 : 2)
+  // into the working ones each plane: k_fast_ws without a source term asks
+  // for it (512^3: 114 GLUP/s against 111.5; by 3 or 4 no gain).  The batch
+  // kernels do not: there it adds spills (k_batch_ws 288 B against 184).
+#pragma unroll (UNROLL)
   for (int k = kb; k < ke; ++k) col.step(un, u, rhs, c0, cx, cy, cz, P, S, k + 1 < ke);
 }
 
