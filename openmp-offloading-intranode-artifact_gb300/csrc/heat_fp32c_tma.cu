@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(NT, 2)
   size_t g = (size_t)(kb - 1) * S + (size_t)gy * P + gx;
   // Unrolled by the intermediate ring's period (3): the slot indices and the
   // shift of the carried values resolve to fixed registers in each copy
-  // (512^3: 325 GLUP/s unrolled by 3, 308 not unrolled, 286 by 2).
+  // (512^3: 325 GLUP/s unrolled by 3, 308 not unrolled, 286 by 2, 321 by 6,
+  // 284 by 12, which spills).
 #pragma unroll 3
   for (int k = kb; k <= ke && !failed; ++k, g += S) {
     wait_plane(k + 2);
