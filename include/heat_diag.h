@@ -4,7 +4,8 @@
  * No counterpart in the reference: the reference measures machine rates with
  * separate microbenchmarks (Kernel-Test/, Bandwidth_Measurements/).  These
  * calls give the FP64 execution-pipe rate of the current device, the ceiling
- * the FP64 stencil forms are held against next to the HBM roofline.
+ * the FP64 stencil forms are held against next to the HBM roofline, and check
+ * the bounded device-side wait behind HEAT_ETIMEOUT.
  */
 #ifndef HEAT_DIAG_H
 #define HEAT_DIAG_H
@@ -27,6 +28,15 @@ int heat_diag_fp64_rate(double *gops_out);
 struct heat_ctx;
 int heat_diag_field_diff(struct heat_ctx *a, struct heat_ctx *b, double *max_abs,
                          double *rel_l2);
+
+/* Bounded-wait check.  One block waits, with the same bounded mbarrier wait
+ * the TMA kernels use (each attempt a try_wait of up to ~2 us), capped at
+ * `attempts` tries (1 .. 2^22, the kernels' own limit; HEAT_EINVAL otherwise),
+ * on an mbarrier that nothing arrives at.  The wait must give
+ * up: *timed_out = 1 and the call returns HEAT_ETIMEOUT, the status a TMA
+ * kernel's context reports when one of its waits runs out, and the device
+ * stays usable.  HEAT_OK with *timed_out = 0 would mean the wait completed. */
+int heat_diag_wait_timeout(unsigned attempts, int *timed_out);
 
 #ifdef __cplusplus
 }

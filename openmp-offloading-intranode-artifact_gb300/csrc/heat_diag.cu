@@ -1,7 +1,8 @@
-// FP64 pipe-rate probe (include/heat_diag.h).
+// FP64 pipe-rate probe and the bounded-wait check (include/heat_diag.h).
 
 #include "heat_diag.h"
 #include "heat_internal.h"
+#include "heat_tma.cuh"
 
 namespace {
 
@@ -13,6 +14,19 @@ __global__ void k_fp64_chains(double *out, double a, double b, int iters) {
     x4 = fma(x4, b, a); x5 = fma(x5, b, a); x6 = fma(x6, b, a); x7 = fma(x7, b, a);
   }
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+// Thread 0 initialises an mbarrier that nothing ever arrives at and waits
+// for its first phase with the bounded wait the TMA kernels use, capped at
+// `attempts` tries; timed_out[0] = 1 when the wait gave up.  No copy is in
+// flight, so giving up leaves nothing behind.
+__global__ void k_wait_unsignalled(unsigned attempts, int *timed_out) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x == 0) {
+    heat::tma::mbar_init(&bar);
+    heat::tma::mbar_init_fence();
+    timed_out[0] = heat::tma::mbar_wait(&bar, 0u, attempts) ? 0 : 1;
+  }
 }
 
 }  // namespace
@@ -53,5 +67,31 @@ done:
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaFree(out);
+  return rc;
+}
+
+extern "C" int heat_diag_wait_timeout(unsigned attempts, int *timed_out) {
+  // at most the TMA kernels' own limit, so the check cannot hold the GPU longer
+  if (!timed_out || attempts == 0 || attempts > heat::tma::kWaitLimit) return HEAT_EINVAL;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ENODEV;
+  }
+  int *d = nullptr, h = -1;
+  if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ENOMEM;
+  }
+  int rc = HEAT_ECUDA;
+  if (cudaMemcpy(d, &h, sizeof(int), cudaMemcpyHostToDevice) == cudaSuccess) {
+    k_wait_unsignalled<<<1, 32>>>(attempts, d);
+    if (cudaGetLastError() == cudaSuccess &&
+        cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess)
+      rc = h == 1 ? HEAT_ETIMEOUT : h == 0 ? HEAT_OK : HEAT_ECUDA;
+  }
+  cudaGetLastError();
+  cudaFree(d);
+  *timed_out = h;
   return rc;
 }

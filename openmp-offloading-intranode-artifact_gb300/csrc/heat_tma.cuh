@@ -1,5 +1,6 @@
 // TMA plane-tile loads and mbarrier waits for kernels that stage plane tiles
-// in shared memory (heat_fp32c_tma.cu).
+// in shared memory (heat_fp32c_tma.cu; the bounded wait is also checked by
+// heat_diag_wait_timeout in heat_diag.cu).
 //
 // A block's thread 0 issues cp.async.bulk.tensor 3-D box loads of plane tiles
 // into a shared-memory ring; each ring slot completes on its own mbarrier
@@ -56,8 +57,11 @@ __device__ __forceinline__ bool mbar_try(unsigned long long *b, unsigned parity)
   return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it)
+// Bounded wait for the phase with the given parity: false when `limit`
+// attempts passed without it completing.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, unsigned parity,
+                                         unsigned limit = kWaitLimit) {
+  for (unsigned it = 0; it < limit; ++it)
     if (mbar_try(b, parity)) return true;
   return false;
 }
