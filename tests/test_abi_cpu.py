@@ -63,6 +63,13 @@ def test_init_rejects_bad_arguments_without_a_device(heat):
     assert lib.heat_step(None, 1) == heat.HEAT_EINVAL
     assert lib.heat_destroy(None) == heat.HEAT_EINVAL
     assert lib.heat_update(None, None, None, None, 4, 4, 4, 0.1, 0) in (heat.HEAT_EINVAL, heat.HEAT_ECUDA)
+    # the bounded-wait check: no output pointer, no attempts, or more attempts than the
+    # kernels' own limit are refused before any device is touched
+    t = C.c_int(-1)
+    assert lib.heat_diag_wait_timeout(10, None) == heat.HEAT_EINVAL
+    assert lib.heat_diag_wait_timeout(0, C.byref(t)) == heat.HEAT_EINVAL
+    assert lib.heat_diag_wait_timeout((1 << 22) + 1, C.byref(t)) == heat.HEAT_EINVAL
+    assert t.value == -1
 
 
 def test_reference_inputs_match_oracle_generator(heat, oracle):
