@@ -1,20 +1,34 @@
 """Benchmark: the FP64 plain heat stencil on the 512^3 configuration.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--skip-cpu] [--skip-batch] [--skip-serve] [--skip-ref-gpu]
 
 Workload (one bench "step"): one 512^3 solve of 1,000 explicit time steps with
 the configuration-1 fields (smooth kappa = 1 + 0.9 sin(2 pi x) sin(4 pi y)
 cos(2 pi z), Gaussian bump u0, zero Dirichlet boundary, dt = 0.9 of the
 stability limit).  Metric: GLUP/s = (nx-2)(ny-2)(nz-2) * time steps / seconds.
 
-  value : device-resident throughput of the default FP64 form through the C
-          ABI (heat_step), timed with CUDA events on the solver's stream, max
-          over ranks.  Each field is 1 GiB, far larger than the 129 MB L2, so
-          no flush is needed between timed steps.
-  e2e   : the same metric through the public ABI from pinned host buffers:
-          heat_init (H2D of kappa and u0) + heat_step + heat_get_field (D2H of
-          u) + heat_destroy, host wall clock.
-  roofline, cpu_baseline, clocks, gpu_launches: see the keys' comments below.
+  value   : device-resident throughput of the default FP64 form through the C
+            ABI (heat_step), timed with CUDA events on the solver's stream, max
+            over ranks.  Each field is 1 GiB, far larger than the 129 MB L2, so
+            no flush is needed between timed steps.
+  e2e     : the same metric through the public ABI from pinned host buffers:
+            heat_init (H2D of kappa and u0) + heat_step + heat_get_field (D2H of
+            u) + heat_destroy, host wall clock; phases_ms splits it by call.
+  fp32c   : the FP32-compensated form on the same inputs: GLUP/s (CUDA events)
+            and its error against the default FP64 form after 100 and 1,000
+            steps (max |u32 - u64| and ||u32 - u64|| / ||u64||, on the device).
+  batch   : configuration 3 (64 uneven grids, half FP64, half FP32C) as one
+            batch: aggregate GLUP/s over the device time of heat_batch_run.
+  serve   : configuration 4's request stream, bounded: 300 requests at a
+            sustainable 10 req/s and 300 at the configured 200 req/s; p50 /
+            p99 / max latency, served GLUP/s, GPU busy fraction, peak HBM.
+  reference_gpu : the reference's own single-GPU CUDA program (1-cuda.cu,
+            its kernel and launch shape, built with its own flags for sm_103a)
+            on the reference problem at 512^3 on the same GPU, when it was built
+            (the fixed-problem program; its GLUP/s is data-independent).
+  roofline, cpu_baseline (all host cores, and serial), clocks, gpu_launches:
+            see the keys' comments below.
 
 --impl reference times the reference's CPU implementation of the loop (the
 oracle restatement in the reference's operation order and OpenMP structure,
@@ -60,6 +74,10 @@ def parse():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--time-steps", type=int, default=TIME_STEPS)
     ap.add_argument("--skip-cpu", action="store_true", help="omit the cpu_baseline leg")
+    ap.add_argument("--skip-batch", action="store_true", help="omit the configuration-3 batch leg")
+    ap.add_argument("--skip-serve", action="store_true", help="omit the configuration-4 serving leg")
+    ap.add_argument("--skip-ref-gpu", action="store_true",
+                    help="omit the timing of the reference's own CUDA program")
     return ap.parse_args()
 
 
@@ -98,12 +116,22 @@ def cpu_sample_steps(n, threads, budget_s):
     return max(2, min(1000, int(budget_s / per)))
 
 
-def cpu_baseline(n, threads):
-    s = cpu_sample_steps(n, threads, 12.0)
+def cpu_baseline(n, threads, budget_s=12.0):
+    s = cpu_sample_steps(n, threads, budget_s)
     r = run_oracle_cli(n, s, threads)
     return {"value": round(r["glups"], 4), "unit": UNIT, "cores": r["threads"], "kind": "port",
             "sample": f"oracle restatement (reference operation order, OpenMP over k), config1 {n}^3, "
                       f"{s} time steps, {r['seconds']:.2f} s"}
+
+
+def cpu_baselines(n):
+    """All host cores (OpenMP-host) and one core (serial), pinned as the
+    reference's run script pins them (OpenMP/run.sh:93-95)."""
+    out = cpu_baseline(n, cpu_threads())
+    ser = cpu_baseline(n, 1, 10.0)
+    out["serial"] = {"value": ser["value"], "unit": UNIT, "cores": 1, "kind": "port",
+                     "sample": ser["sample"]}
+    return out
 
 
 def reference_arm(a):
@@ -136,18 +164,64 @@ def reference_arm(a):
 
 # ---------------------------------------------------------------- clocks
 # ---------------------------------------------------------------- our arm
-def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    p = ROOT / "profiles" / "fp64_default_512.md"
-    if not p.exists():
-        return None
-    for ln in p.read_text().splitlines():
-        if ln.startswith("traffic_bytes_per_launch:"):
-            try:
-                return float(ln.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+REF_CUDA = ROOT / "oracle" / "_ref" / "1-cuda"
+REF_CUDA_FLAGS = "-O3 --fmad=false --prec-div=true --prec-sqrt=true --ftz=false -arch=sm_103a -Xcompiler -fopenmp"
+
+
+def reference_gpu_leg(n=512, steps=300):
+    """The reference's own single-GPU CUDA program (1-cuda.cu, unmodified; built
+    by oracle/build_ref.sh with the reference Makefile's flags, -arch changed
+    to sm_103a) on this GPU: its fixed problem at n^3 for `steps` steps.  T is
+    chosen so that the program's own `while (t < T) t += dt` loop takes `steps`
+    steps; GLUP/s from its printed `Time = ... seconds` (omp_get_wtime around
+    the loop and the final cudaDeviceSynchronize, 1-cuda.cu:231-257)."""
+    if not REF_CUDA.exists():
+        return {"unavailable": "oracle/_ref/1-cuda not built (the reference's 1-cuda.cu is staged "
+                               "by oracle/build_ref.sh where the reference tree is present)"}
+    h = 1.0 / (n - 1)
+    dt = h * h / (12.0 * 0.95)            # 1-cuda.cu:150-152
+    T = (steps - 0.5) * dt
+    t, expect = 0.0, 0
+    while t < T:                           # the program's own step count (1-cuda.cu:238-250)
+        t += dt
+        expect += 1
+    w0 = time.perf_counter()
+    r = subprocess.run([str(REF_CUDA), str(n), repr(T)], capture_output=True, text=True,
+                       env={**os.environ, "WRITE_TXT": "0"}, timeout=900)
+    wall = time.perf_counter() - w0
+    if r.returncode != 0:
+        return {"error": f"1-cuda exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+    got_steps = secs = None
+    for ln in r.stdout.splitlines():
+        if ln.strip().endswith("timesteps complete"):
+            got_steps = int(ln.split()[0])
+        if ln.startswith("Time = "):
+            secs = float(ln.split()[2])
+    if got_steps is None or not secs:
+        return {"error": "could not parse the program's output"}
+    v = (n - 2) ** 3 * got_steps / secs / 1e9
+    return {"value": round(v, 3), "unit": UNIT, "n": n, "time_steps": got_steps,
+            "expected_time_steps": expect, "seconds": secs, "wall_s": round(wall, 1),
+            "vs_h100_published": round(v / H100_1CUDA_N512, 3),
+            "program": "reference 1-cuda.cu, unmodified, its own problem (rhs term, kappa = 0.5+0.45 sin sin sin)",
+            "build": f"nvcc {REF_CUDA_FLAGS} -lm"}
+
+
+TRAFFIC_RECORD = ROOT / "profiles" / "fp64_default_traffic.json"
+
+
+def profile_traffic(updates_per_launch):
+    """DRAM bytes (read + write) per launch of the dominant kernel: the
+    machine-readable record of one ncu capture (its command and raw
+    dram__bytes_read.sum / dram__bytes_write.sum of the captured launch),
+    scaled from the captured launch's updates to this launch's."""
+    if not TRAFFIC_RECORD.exists():
+        return None, None
+    rec = json.loads(TRAFFIC_RECORD.read_text())
+    cap = rec["capture"]
+    per_update = (cap["dram_bytes_read"] + cap["dram_bytes_write"]) / cap["updates"]
+    return per_update * updates_per_launch, {"kernel": rec["kernel"], "bytes_per_update": round(per_update, 2),
+                                             "captured": cap["case"]}
 
 
 def max_over_ranks(x, dist, device):
@@ -216,17 +290,26 @@ def our_arm(a):
     l2n, csum = s.norm()
     s.close()
 
-    # ---- FP32-compensated form on the same workload (precision pattern)
-    s32 = H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C, stream=stream.cuda_stream)
-    s32.step(max(1, ts // 10))
-    s32.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    s32.step(ts)
-    e1.record(stream)
-    e1.synchronize()
-    ms32 = e0.elapsed_time(e1)
-    s32.close()
+    # ---- FP32-compensated form on the same inputs (precision pattern):
+    # rate by CUDA events, error against the default FP64 form at 100 and ts
+    # steps (field difference on the device)
+    f64 = H.Solver(kappa, u0, h, dt, stream=stream.cuda_stream)
+    f32 = H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C, stream=stream.cuda_stream)
+    ms32, done, fp32c_err = 0.0, 0, []
+    for cp in sorted({min(100, ts), ts}):
+        k = cp - done
+        f64.step(k)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        f32.step(k)
+        e1.record(stream)
+        e1.synchronize()
+        ms32 += e0.elapsed_time(e1)
+        mx, rl = H.field_diff(f32, f64)
+        fp32c_err.append({"steps": cp, "rel_l2": rl, "max_abs": mx})
+        done = cp
+    f32.close()
+    f64.close()
     fp32c_value = updates(n, ts) / (ms32 * 1e-3) / 1e9
     t_max = max_over_ranks(ms, dist, "cuda")
     upd = updates(n, ts) * a.steps
@@ -234,7 +317,7 @@ def our_arm(a):
     launch_ms = ms / (a.steps * ts)
     achieved_gbs = updates(n, 1) * BYTES_PER_UPDATE / (launch_ms * 1e-3) / 1e9
 
-    # ---- end to end through the ABI from pinned host memory
+    # ---- end to end through the ABI from pinned host memory, timed per call
     pk = torch.empty(kappa.shape, dtype=torch.float64, pin_memory=True)
     pu = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
     pout = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
@@ -242,25 +325,59 @@ def our_arm(a):
     pu.numpy()[...] = u0
     del kappa, u0
     e2e_steps = max(1, min(a.steps, 3))
+    phase_names = ("heat_init", "heat_step", "heat_get_field", "heat_destroy")
+    phases = dict.fromkeys(phase_names, 0.0)
     with ClockSampler(dev) as e2e_clk:
         for i in range(e2e_steps + 1):   # first one is warm-up
             barrier()
-            t0 = time.perf_counter()
-            with H.Solver(pk.numpy(), pu.numpy(), h, dt, stream=stream.cuda_stream) as e:
-                e.step(ts)
-                e.field(pout.numpy())
-            t1 = time.perf_counter()
-            if i == 0:
-                e2e_t = 0.0
-            else:
-                e2e_t += t1 - t0
+            t = [time.perf_counter()]
+            e = H.Solver(pk.numpy(), pu.numpy(), h, dt, stream=stream.cuda_stream)
+            t.append(time.perf_counter())
+            e.step(ts)
+            e.sync()                      # steps done (heat_get_field would wait for them anyway)
+            t.append(time.perf_counter())
+            e.field(pout.numpy())
+            t.append(time.perf_counter())
+            e.close()
+            t.append(time.perf_counter())
+            if i > 0:
+                for nm, a0, a1 in zip(phase_names, t, t[1:]):
+                    phases[nm] += a1 - a0
+    e2e_t = sum(phases.values())
     e2e_s = max_over_ranks(e2e_t / e2e_steps, dist, "cuda")
     e2e_value = replica_value(updates(n, ts), world, e2e_s)
+
+    # ---- configuration 3 (batch) and configuration 4 (serving), bounded
+    batch_out = serve_out = ref_gpu = None
+    if rank == 0 and not a.skip_batch:
+        try:
+            import batch_bench
+            r = batch_bench.run(tune=True)
+            batch_out = {"value": r["batch_glups"], "unit": UNIT, "workload": r["workload"],
+                         "updates": r["updates"], "device_ms": r["batch_ms"],
+                         "kernel_launches": r["kernel_launches"], "graph_launches": r["graph_launches"],
+                         "clocks": r["clocks"]}
+        except Exception as ex:  # report, do not hide
+            batch_out = {"error": str(ex)}
+    if rank == 0 and not a.skip_serve:
+        try:
+            import serve_bench
+            serve_out = {}
+            for key, nreq, rate in (("sustainable", 300, 10.0), ("configured_rate", 300, 200.0)):
+                r = serve_bench.run(requests=nreq, rate=rate, device=dev)
+                serve_out[key] = {k: r[k] for k in (
+                    "workload", "offered_glups", "glups", "p50_ms", "p99_ms", "max_ms",
+                    "p50_ms_fp64", "p99_ms_fp64", "p50_ms_fp32c", "p99_ms_fp32c", "completed",
+                    "rejected", "gpu_busy_frac", "peak_gb", "wall_s", "clocks")}
+        except Exception as ex:
+            serve_out = {"error": str(ex)}
+    if rank == 0 and not a.skip_ref_gpu:
+        ref_gpu = reference_gpu_leg()
 
     if rank == 0:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
         hbm_peak = peaks.get("hbm_gbs", 6800.0)
-        traffic = profile_traffic()
+        traffic, traffic_src = profile_traffic(updates(n, 1))
         out = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(t_max / a.steps, 3),
@@ -273,29 +390,37 @@ def our_arm(a):
             "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(achieved_gbs / hbm_peak, 4),
                          "peak_source": "measured" if peaks else "fallback",
-                         "traffic": traffic, "bytes_per_update": BYTES_PER_UPDATE,
+                         "traffic": traffic, "traffic_source": traffic_src,
+                         "bytes_per_update": BYTES_PER_UPDATE,
                          "kernel_ms_per_launch": round(launch_ms, 4),
                          "fp64_pipe": {"peak_gops": round(fp64_peak, 1),
                                        "note": "measured FP64 FMA rate of this GPU (heat_diag_fp64_rate)"}},
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT,
                     "h2d_bytes_per_step": int(pk.numel() * 8 + pu.numel() * 8),
                     "d2h_bytes_per_step": int(pout.numel() * 8),
-                    "ms_per_step": round(e2e_s * 1e3, 3), "clocks": e2e_clk.summary()},
+                    "ms_per_step": round(e2e_s * 1e3, 3),
+                    "phases_ms": {k: round(v * 1e3 / e2e_steps, 3) for k, v in phases.items()},
+                    "clocks": e2e_clk.summary()},
             "fp32c": {"value": round(fp32c_value, 3), "unit": UNIT,
                       "vs_fp64": round(fp32c_value / (value / world), 3),
                       "bytes_per_update": FP32C_BYTES_PER_UPDATE_TB2,
                       "hbm_frac": round(fp32c_value * FP32C_BYTES_PER_UPDATE_TB2 / hbm_peak, 4),
                       "hbm_frac_single_step_bytes": round(fp32c_value * FP32C_BYTES_PER_UPDATE / hbm_peak, 4),
+                      "error_vs_fp64": fp32c_err,
                       "note": "FP32 u + BF16 Kahan carry, FP32 face weights, two steps per launch "
-                              "(TMA-staged temporal blocking); same workload, "
-                              f"{ts} steps, CUDA events; errors: profiles/fp32c_precision.md"},
+                              "(TMA-staged temporal blocking); same inputs, "
+                              f"{ts} steps, CUDA events; error against the default FP64 form "
+                              "(itself within 1e-12 of the reference)"},
+            "batch": batch_out,
+            "serve": serve_out,
+            "reference_gpu": ref_gpu,
             "gpu_launches": int(l1 - l0),
             "clocks": clk.summary(),
             "result": {"l2": l2n, "checksum": csum},
         }
         if not a.skip_cpu:
             try:
-                out["cpu_baseline"] = cpu_baseline(n, cpu_threads())
+                out["cpu_baseline"] = cpu_baselines(n)
             except Exception as ex:  # report, do not hide
                 out["cpu_baseline"] = {"error": str(ex)}
         print(json.dumps(out), flush=True)

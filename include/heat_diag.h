@@ -38,6 +38,18 @@ int heat_diag_field_diff(struct heat_ctx *a, struct heat_ctx *b, double *max_abs
  * stays usable.  HEAT_OK with *timed_out = 0 would mean the wait completed. */
 int heat_diag_wait_timeout(unsigned attempts, int *timed_out);
 
+/* Failure path of the product kernel itself.  Queues, on the context's
+ * stream, one launch of the FP32C two-step kernel (the kernel heat_step uses
+ * for HEAT_FP32C contexts) with its wait limit set to 0 attempts: its first
+ * mbarrier wait gives up at once, it sets the context's error flag, waits
+ * (with the full bounded wait) for its own loads in flight and returns
+ * without writing any point.  The context's fields and step count are
+ * unchanged.  The next call that synchronises the context -- heat_sync,
+ * heat_norm, heat_get_field, or heat_batch_run of a batch holding it --
+ * returns HEAT_ETIMEOUT, once.  HEAT_ESTATE for a context that does not step
+ * with the two-step kernel (HEAT_FP64, a source term, HEAT_NO_TEMPORAL).    */
+int heat_diag_fp32c_timeout(struct heat_ctx *c);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,29 +27,29 @@ import heat_ctypes as H  # noqa: E402
 from clocks import ClockSampler  # noqa: E402
 
 
-def main() -> None:
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--grids", type=int, default=64)
-    ap.add_argument("--seed", type=int, default=3)
-    ap.add_argument("--min-axis", type=int, default=48)
-    ap.add_argument("--max-axis", type=int, default=384)
-    ap.add_argument("--min-steps", type=int, default=200)
-    ap.add_argument("--max-steps", type=int, default=2000)
-    ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--skip-sequential", action="store_true")
-    a = ap.parse_args()
+def specs_config3(grids: int = 64, seed: int = 3, min_axis: int = 48, max_axis: int = 384,
+                  min_steps: int = 200, max_steps: int = 2000) -> list[dict]:
+    """The grids of configuration 3: shapes, seeds, step counts and forms."""
+    rng = random.Random(seed)
+    specs = []
+    for g in range(grids):
+        shape = tuple(rng.randint(min_axis, max_axis) for _ in range(3))
+        specs.append({"shape": shape, "seed": 1000 * seed + g, "steps": rng.randint(min_steps, max_steps),
+                      "precision": H.HEAT_FP64 if g % 2 == 0 else H.HEAT_FP32C})
+    return specs
+
+
+def run(grids: int = 64, seed: int = 3, min_axis: int = 48, max_axis: int = 384,
+        min_steps: int = 200, max_steps: int = 2000, tune: bool = True,
+        sequential: bool = False) -> dict:
+    """Run configuration 3 once as one batch; returns the JSON record."""
     import torch
 
-    rng = random.Random(a.seed)
-    specs = []
-    for g in range(a.grids):
-        shape = tuple(rng.randint(a.min_axis, a.max_axis) for _ in range(3))
-        specs.append({"shape": shape, "seed": 1000 * a.seed + g, "steps": rng.randint(a.min_steps, a.max_steps),
-                      "precision": H.HEAT_FP64 if g % 2 == 0 else H.HEAT_FP32C})
+    specs = specs_config3(grids, seed, min_axis, max_axis, min_steps, max_steps)
     t0 = time.perf_counter()
-    if not a.no_tune:
-        H.tune_batch(H.HEAT_FP64, 0, max_nz=a.max_axis)
-        H.tune_batch(H.HEAT_FP32C, 0, max_nz=a.max_axis)
+    if tune:
+        H.tune_batch(H.HEAT_FP64, 0, max_nz=max_axis)
+        H.tune_batch(H.HEAT_FP32C, 0, max_nz=max_axis)
     tune_s = time.perf_counter() - t0
 
     stream = torch.cuda.Stream()
@@ -75,14 +75,14 @@ def main() -> None:
     ms = e0.elapsed_time(e1)
     launches, graphs, _ = batch.stats()
     batch.close()
-    out = {"workload": f"config3: {a.grids} grids, axes U{{{a.min_axis}..{a.max_axis}}}, steps "
-                       f"U[{a.min_steps},{a.max_steps}], half FP64 / half FP32C",
+    out = {"workload": f"config3: {grids} grids, axes U{{{min_axis}..{max_axis}}}, steps "
+                       f"U[{min_steps},{max_steps}], half FP64 / half FP32C",
            "updates": updates, "batch_ms": round(ms, 2), "batch_glups": round(updates / (ms * 1e-3) / 1e9, 2),
            "batch_steps": taken, "kernel_launches": launches, "graph_launches": graphs,
            "tune_s": round(tune_s, 2), "setup_s": round(setup_s, 2),
            "kchunks": {str(n): H.tune_lookup(p, 0, n) for p in (0, 1) for n in (64, 128, 256, 384)},
            "clocks": clk.summary()}
-    if not a.skip_sequential:
+    if sequential:
         # the same work, one context at a time with heat_step (fresh contexts)
         seq_ms = 0.0
         for sp in specs:
@@ -99,6 +99,22 @@ def main() -> None:
         out["sequential_glups"] = round(updates / (seq_ms * 1e-3) / 1e9, 2)
     for s in solvers:
         s.close()
+    return out
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--grids", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=3)
+    ap.add_argument("--min-axis", type=int, default=48)
+    ap.add_argument("--max-axis", type=int, default=384)
+    ap.add_argument("--min-steps", type=int, default=200)
+    ap.add_argument("--max-steps", type=int, default=2000)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--skip-sequential", action="store_true")
+    a = ap.parse_args()
+    out = run(a.grids, a.seed, a.min_axis, a.max_axis, a.min_steps, a.max_steps,
+              tune=not a.no_tune, sequential=not a.skip_sequential)
     print(json.dumps(out), flush=True)
 
 

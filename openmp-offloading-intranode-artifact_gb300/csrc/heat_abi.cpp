@@ -20,10 +20,9 @@ thread_local char g_last_error[256] = "";
 // the others run the integer-pipe evaluation.
 constexpr int kDefaultHwRows = 4;
 
-int cuda_fail(cudaError_t e, const char *what) {
-  std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
-  return HEAT_ECUDA;
-}
+using heat::check_err;
+using heat::cuda_fail;
+using heat::two_step_form;
 
 #define CK(call)                                        \
   do {                                                  \
@@ -148,13 +147,9 @@ cudaError_t enqueue_one(heat_ctx *c, int cur, cudaStream_t st) {
   if (c->flags & HEAT_NAIVE) return heat::launch_naive(un, uo, c->rhs, c->kappa, g, c->factor, st);
   if (c->flags & HEAT_BITEXACT)
     return heat::launch_exact_faces(un, uo, c->rhs, c->ks, g, c->factor, st);
-  if (c->kq) return heat::launch_fast_mix(un, uo, c->rhs, c->kq, c->c0, c->cf, g, c->hw_rows, st);
-  return heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, st, true);
-}
-
-bool two_step_form(const heat_ctx *c) {
-  return c->precision == HEAT_FP32C && !c->frhs && !(c->flags & HEAT_NO_TEMPORAL) &&
-         heat::fp32c_tb2_ok(c->g);
+  if (c->kq)
+    return heat::launch_fast_mix(un, uo, c->rhs, c->kq, c->c0, c->cf, g, c->hw_rows, c->err, st);
+  return heat::launch_fast(un, uo, c->rhs, c->c0, c->cf, g, st);
 }
 
 int launch_step(heat_ctx *c) {
@@ -163,19 +158,6 @@ int launch_step(heat_ctx *c) {
   c->launches += 1;
   c->cur ^= 1;
   c->steps_done += 1;
-  return HEAT_OK;
-}
-
-// HEAT_ETIMEOUT if a kernel of this context reported a bounded wait running
-// out (the flag is cleared once reported).  Synchronises the stream.
-int check_err(heat_ctx *c) {
-  int flag = 0;
-  CK(cudaMemcpyAsync(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  if (flag) {
-    CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
-    return HEAT_ETIMEOUT;
-  }
   return HEAT_OK;
 }
 
@@ -402,6 +384,28 @@ done:
 
 namespace heat {
 
+int cuda_fail(cudaError_t e, const char *what) {
+  std::snprintf(g_last_error, sizeof g_last_error, "%s: %s", what, cudaGetErrorString(e));
+  return HEAT_ECUDA;
+}
+
+bool two_step_form(const heat_ctx *c) {
+  return c->precision == HEAT_FP32C && !c->frhs && !(c->flags & HEAT_NO_TEMPORAL) &&
+         fp32c_tb2_ok(c->g);
+}
+
+int check_err(heat_ctx *c) {
+  int flag = 0;
+  CK(cudaMemcpyAsync(&flag, c->err, sizeof flag, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (flag) {
+    CK(cudaMemsetAsync(c->err, 0, sizeof(int), c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return HEAT_ETIMEOUT;
+  }
+  return HEAT_OK;
+}
+
 cudaError_t enqueue_ctx_steps(heat_ctx *c, int cur, long long n, cudaStream_t st,
                               long long *launches) {
   long long s = 0;
@@ -547,13 +551,15 @@ int heat_norm(heat_ctx *c, double *l2, double *checksum) {
   return HEAT_OK;
 }
 
+// The field is copied out even when a kernel's bounded wait ran out, but the
+// call then returns HEAT_ETIMEOUT: the copy holds whatever that launch left.
 int heat_get_field(heat_ctx *c, double *u_host) {
   if (!c || !u_host) return HEAT_EINVAL;
   if (c->precision == HEAT_FP64) {
     int rc = download(u_host, c->u[c->cur], c->g, c->stream);
     if (rc != HEAT_OK) return rc;
     CK(cudaStreamSynchronize(c->stream));
-    return HEAT_OK;
+    return check_err(c);
   }
   double *tmp = nullptr;
   int rc = widen_current(c, &tmp);
@@ -562,7 +568,7 @@ int heat_get_field(heat_ctx *c, double *u_host) {
   if (tmp) cudaFreeAsync(tmp, c->stream);
   if (rc != HEAT_OK) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "heat_get_field");
-  return HEAT_OK;
+  return check_err(c);
 }
 
 int heat_set_field(heat_ctx *c, const double *u_host) {
@@ -634,6 +640,20 @@ int heat_update(double *u_new, const double *u_old, const double *rhs, const dou
     if (cur != device_id) CK(cudaSetDevice(device_id));
   }
   return heat_update_async(u_new, u_old, rhs, kappa, nz, ny, nx, factor, (void *)cudaStreamLegacy);
+}
+
+int heat_diag_fp32c_timeout(heat_ctx *c) {
+  if (!c) return HEAT_EINVAL;
+  if (!two_step_form(c)) return HEAT_ESTATE;
+  // The product two-step kernel with a wait limit of 0 attempts: its first
+  // wait gives up, it sets the context's error flag, drains its own loads in
+  // flight (with the full bounded wait) and returns without writing a point.
+  // The context's buffers and step count are left as they were.
+  cudaError_t e = heat::launch_fp32c_tb2(c->v[c->cur ^ 1], c->carry[c->cur ^ 1], c->v[c->cur],
+                                         c->carry[c->cur], c->fcf, c->g, c->err, c->stream, 0u);
+  if (e != cudaSuccess) return cuda_fail(e, "two-step kernel launch");
+  c->launches += 1;
+  return HEAT_OK;
 }
 
 int heat_diag_field_diff(heat_ctx *a, heat_ctx *b, double *max_abs, double *rel_l2) {

@@ -591,6 +591,15 @@ int batch_run(heat_batch *b, long long max_steps, long long *steps_taken, bool s
     cudaGetLastError();
     if (rc == HEAT_OK) rc = HEAT_ECUDA;
   }
+  // A member whose TMA-staged launches (the kernels with device-side waits:
+  // FP32C two-step, default FP64) reported a wait running out makes the run
+  // return HEAT_ETIMEOUT; every member's flag is read (and cleared) so none is
+  // reported twice.
+  if (sync)
+    for (auto &en : b->entries) {
+      const int e = check_err(en.ctx);
+      if (rc == HEAT_OK && e != HEAT_OK) rc = e;
+    }
   if (steps_taken) *steps_taken = done;
   return rc;
 }

@@ -87,7 +87,7 @@ struct Maps {
 __global__ void __launch_bounds__(NT, 2)
     k_fp32c_tb2(const __grid_constant__ Maps in, float *__restrict__ vn,
                 uint16_t *__restrict__ cn, int nx, int ny, int nz, int P, size_t S, int kchunk,
-                int *__restrict__ err) {
+                int *__restrict__ err, unsigned wait_limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(NT, 2)
   auto wait_plane = [&](int p) {
     if (!waiter || p < pmin || p > pmax || failed) return;
     const int s = p & (R - 1);
-    if (!mbar_wait(&sm.bar[s], (phase >> s) & 1u)) {
+    if (!mbar_wait(&sm.bar[s], (phase >> s) & 1u, wait_limit)) {
       failed = true;
       return;
     }
@@ -313,7 +313,9 @@ bool fp32c_tb2_ok(const heat_geom &g) {
 }
 
 cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
-                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st) {
+                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st,
+                             unsigned wait_limit) {
+  if (wait_limit > tma::kWaitLimit) wait_limit = tma::kWaitLimit;
   Maps m;
   if (!encode(&m.v, v, false, g) || !encode(&m.c, cr, true, g) || !encode(&m.wx, w[0], false, g) ||
       !encode(&m.wy, w[1], false, g) || !encode(&m.wz, w[2], false, g))
@@ -328,7 +330,7 @@ cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, cons
   const int kchunk = (int)((interior + chunks - 1) / chunks);
   dim3 grid(bx, by, (interior + kchunk - 1) / kchunk);
   k_fp32c_tb2<<<grid, NT, fp32c_tb2_smem(), st>>>(m, v_new, c_new, g.nx, g.ny, g.nz, g.pitch,
-                                                  g.plane, kchunk, err);
+                                                  g.plane, kchunk, err, wait_limit);
   return cudaGetLastError();
 }
 

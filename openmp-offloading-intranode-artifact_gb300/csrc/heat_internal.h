@@ -61,6 +61,11 @@ namespace heat {
 
 constexpr int kNormBlocks = 152 * 4;   // partial-sum blocks of the norm pass
 
+// Bound of every device-side mbarrier wait in the TMA kernels (try_wait
+// attempts, each suspending up to ~2 us); a wait that runs out sets the
+// context's error flag and the launch returns with its outputs unwritten.
+constexpr unsigned kWaitLimit = 1u << 22;
+
 // Planes per block for a launch of (tile_x x tile_y)-column tiles over the
 // grid's interior: enough z-chunks that tiles x chunks reaches `want` blocks
 // (16 per SM of GB300's 152 by default), at least 8 planes each.
@@ -93,17 +98,26 @@ cudaError_t launch_fast_coeffs(double *c0, double *const cf[3], const double *ka
                                const heat_geom &g, double factor, cudaStream_t st);
 cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
                         const double *c0, double *const cf[3], const heat_geom &g,
-                        cudaStream_t st, bool hw_only);
+                        cudaStream_t st);
 
 // heat_fp64_int.cu
 cudaError_t launch_kq_setup(unsigned long long *K, int *bad, const double *kappa,
                             const heat_geom &g, double factor, cudaStream_t st);
 // hw_rows of the 8 warps in each block take the FP64 pipe, the rest the
 // integer pipes; K may be NULL only when hw_rows == 8, c0/cf only when 0.
+// err: the context's flag, set when a bounded wait of the TMA-staged kernel
+// runs out (HEAT_ETIMEOUT).
 cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rhs,
                             const unsigned long long *K, const double *c0,
                             double *const cf[3], const heat_geom &g, int hw_rows,
-                            cudaStream_t st);
+                            int *err, cudaStream_t st);
+
+// heat_fp64_tma.cu: the hw_rows = 4, no-source-term split with the integer
+// rows' plane tiles staged by TMA (bit-identical to the k_fast_ws launch).
+bool fast_tma_usable(const heat_geom &g);
+cudaError_t launch_fast_tma(double *u_new, const double *u_old, const unsigned long long *K,
+                            const double *c0, double *const cf[3], const heat_geom &g, int *err,
+                            cudaStream_t st, unsigned wait_limit = kWaitLimit);
 // n steps of context c from buffer `cur` on stream st with its own
 // single-grid kernels (two steps per launch where its form has them); the
 // context's bookkeeping is untouched.  ctx_flips gives the parity of buffer
@@ -124,9 +138,19 @@ cudaError_t launch_f32_weights(float *const w[3], const double *kappa, const hea
 cudaError_t launch_to_f32(float *o, const double *a, size_t total, cudaStream_t st);
 
 // heat_fp32c_tma.cu: two steps per launch (temporal blocking, TMA staging).
+// wait_limit bounds every mbarrier wait of the launch (kWaitLimit in product
+// use; smaller only to exercise the failure path).
 bool fp32c_tb2_ok(const heat_geom &g);
 cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
-                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st);
+                             float *const w[3], const heat_geom &g, int *err, cudaStream_t st,
+                             unsigned wait_limit = kWaitLimit);
+// Whether a context steps with launch_fp32c_tb2.
+bool two_step_form(const heat_ctx *c);
+// HEAT_ETIMEOUT if a kernel of context c reported a bounded wait running out
+// (the flag is cleared once reported), else HEAT_OK.  Synchronises c's stream.
+int check_err(heat_ctx *c);
+// Record a failed CUDA call for heat_strerror() and return HEAT_ECUDA.
+int cuda_fail(cudaError_t e, const char *what);
 
 // heat_reduce.cu
 cudaError_t launch_norm_f64(const double *u, const heat_geom &g, double *partials,

@@ -10,20 +10,27 @@
 // which owns a scratch buffer allocated at heat_init(); this variant keeps its
 // scratch in a fixed static device array instead.
 //
-// Scratch: g_norm_scratch holds one (sum, sum of squares) pair per plane plus
-// the final pair -- 2 * HEAT_NORM_NOALLOC_MAX_NZ + 2 doubles (256 KiB), held by
-// every GPU that loads the library until the process exits.  Fields with more
-// than HEAT_NORM_NOALLOC_MAX_NZ planes are rejected with HEAT_EINVAL.
+// Scratch: g_norm_scratch holds one (sum, sum of squares) pair per partial
+// sum plus the final pair -- 2 * kSlots + 2 doubles (256 KiB), held by every
+// GPU that loads the library until the process exits.  Each plane is cut into
+// C chunks (as many as keep about 8 blocks per SM busy, within kSlots / nz),
+// one block per (chunk, plane), so a shallow, wide field uses the whole GPU.
+// Fields with more than HEAT_NORM_NOALLOC_MAX_NZ (= kSlots) planes are
+// rejected with HEAT_EINVAL.
 //
 // Host code cannot use g_norm_scratch's name as a device address (on the host
 // it names a shadow variable).  The first call on each device, with that
-// device current, looks the address up with cudaGetSymbolAddress and caches it
-// per device; make that first call on a device before any stream capture.
-// Every call on a device shares the array and it keeps the last call's
-// contents; each pass writes every slot it later reads, so nothing has to be
-// cleared.  Calls that overlap on the same GPU race on the array: issue them
-// from one stream, or order them on the host.
+// device current, looks the address up with cudaGetSymbolAddress and keeps it
+// for that device once the lookup succeeded (a failed lookup is reported and
+// tried again on the next call); make that first call on a device before any
+// stream capture.  A cudaDeviceReset() of the device releases the array and
+// the kept address with it: do not call this entry point on a device after
+// resetting it in the same process.  Every call on a device shares the array
+// and it keeps the last call's contents; each pass writes every slot it later
+// reads, so nothing has to be cleared.  Calls that overlap on the same GPU
+// race on the array: issue them from one stream, or order them on the host.
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -31,11 +38,12 @@
 
 namespace {
 
-constexpr int kMaxNz = HEAT_NORM_NOALLOC_MAX_NZ;
+constexpr int kSlots = HEAT_NORM_NOALLOC_MAX_NZ;  // partial-sum pairs
 constexpr int kThreads = 256;
 constexpr int kMaxDevices = 64;
+constexpr int kWantBlocks = 152 * 8;  // about 8 blocks per SM of GB300
 
-static __device__ __align__(256) double g_norm_scratch[2 * kMaxNz + 2];
+static __device__ __align__(256) double g_norm_scratch[2 * kSlots + 2];
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -59,71 +67,99 @@ __device__ __forceinline__ void block_sum2(double &a, double &b) {
   }
 }
 
-// One block per plane: scratch[2k], scratch[2k+1] = sum u, sum u^2 of plane k.
+// Block (x, k) sums points [x * chunk, min((x + 1) * chunk, plane)) of plane k
+// into slot k * gridDim.x + x: scratch[2 slot] = sum u, [2 slot + 1] = sum u^2.
 __global__ void __launch_bounds__(kThreads)
-    k_plane_sums(const double *__restrict__ u, int ny, int nx, double *__restrict__ scratch) {
-  const size_t plane = (size_t)ny * nx;
-  const double *p = u + (size_t)blockIdx.x * plane;
+    k_chunk_sums(const double *__restrict__ u, size_t plane, size_t chunk,
+                 double *__restrict__ scratch) {
+  const double *p = u + (size_t)blockIdx.y * plane;
+  const size_t b = (size_t)blockIdx.x * chunk;
+  const size_t e = b + chunk < plane ? b + chunk : plane;
   double s = 0.0, q = 0.0;
-  for (size_t t = threadIdx.x; t < plane; t += kThreads) {
+  for (size_t t = b + threadIdx.x; t < e; t += kThreads) {
     const double x = p[t];
     s += x;
     q = fma(x, x, q);
   }
   block_sum2(s, q);
   if (threadIdx.x == 0) {
-    scratch[2 * blockIdx.x] = s;
-    scratch[2 * blockIdx.x + 1] = q;
+    const size_t slot = (size_t)blockIdx.y * gridDim.x + blockIdx.x;
+    scratch[2 * slot] = s;
+    scratch[2 * slot + 1] = q;
   }
 }
 
-// Fold the nz plane pairs in index order into scratch[2*kMaxNz], [2*kMaxNz+1].
-__global__ void __launch_bounds__(kThreads) k_fold(double *__restrict__ scratch, int nz) {
+// Fold the first nslots pairs (each thread its strided share in index order,
+// then a fixed tree) into scratch[2 * kSlots], [2 * kSlots + 1].
+__global__ void __launch_bounds__(kThreads) k_fold(double *__restrict__ scratch, int nslots) {
   double s = 0.0, q = 0.0;
-  for (int k = threadIdx.x; k < nz; k += kThreads) {
+  for (int k = threadIdx.x; k < nslots; k += kThreads) {
     s += scratch[2 * k];
     q += scratch[2 * k + 1];
   }
   block_sum2(s, q);
   if (threadIdx.x == 0) {
-    scratch[2 * kMaxNz] = s;
-    scratch[2 * kMaxNz + 1] = q;
+    scratch[2 * kSlots] = s;
+    scratch[2 * kSlots + 1] = q;
   }
 }
 
+// The scratch array's device address on each device, kept once looked up.
 struct DeviceScratch {
-  std::once_flag once;
+  std::mutex mu;
   double *ptr = nullptr;
-  cudaError_t err = cudaSuccess;
 };
 DeviceScratch g_scratch[kMaxDevices];
+
+int scratch_address(int dev, double **out) {
+  DeviceScratch &ds = g_scratch[dev];
+  std::lock_guard<std::mutex> lk(ds.mu);
+  if (!ds.ptr) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_norm_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return heat::cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                             "heat_norm_noalloc: cudaGetSymbolAddress of its scratch");
+    }
+    ds.ptr = static_cast<double *>(p);
+  }
+  *out = ds.ptr;
+  return HEAT_OK;
+}
 
 }  // namespace
 
 extern "C" int heat_norm_noalloc(const double *u, int nz, int ny, int nx, double *l2,
                                  double *checksum, void *stream) {
   if (!u || nz < 1 || ny < 1 || nx < 1) return HEAT_EINVAL;
-  if (nz > kMaxNz) return HEAT_EINVAL;  // beyond the static scratch
+  if (nz > kSlots) return HEAT_EINVAL;  // beyond the static scratch
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
     return HEAT_ENODEV;
   }
-  DeviceScratch &ds = g_scratch[dev];
-  std::call_once(ds.once, [&ds] {
-    ds.err = cudaGetSymbolAddress(reinterpret_cast<void **>(&ds.ptr), g_norm_scratch);
-  });
-  if (ds.err != cudaSuccess || !ds.ptr) return HEAT_ECUDA;
+  double *scratch = nullptr;
+  if (int rc = scratch_address(dev, &scratch)) return rc;
+  const size_t plane = (size_t)ny * nx;
+  // Chunks per plane: enough blocks to fill the GPU, within the slots, and no
+  // more chunks than a plane has block-sized pieces.
+  long chunks = (kWantBlocks + nz - 1) / nz;
+  chunks = std::min<long>(chunks, kSlots / nz);
+  chunks = std::min<long>(chunks, (long)((plane + kThreads - 1) / kThreads));
+  chunks = std::max<long>(chunks, 1);
+  const size_t chunk = (plane + chunks - 1) / chunks;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_plane_sums<<<nz, kThreads, 0, st>>>(u, ny, nx, ds.ptr);
-  k_fold<<<1, kThreads, 0, st>>>(ds.ptr, nz);
-  if (cudaGetLastError() != cudaSuccess) return HEAT_ECUDA;
+  k_chunk_sums<<<dim3((unsigned)chunks, (unsigned)nz), kThreads, 0, st>>>(u, plane, chunk, scratch);
+  k_fold<<<1, kThreads, 0, st>>>(scratch, (int)(chunks * nz));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return heat::cuda_fail(e, "heat_norm_noalloc launch");
   double r[2];
-  if (cudaMemcpyAsync(r, ds.ptr + 2 * kMaxNz, sizeof r, cudaMemcpyDeviceToHost, st) !=
-          cudaSuccess ||
-      cudaStreamSynchronize(st) != cudaSuccess) {
+  e = cudaMemcpyAsync(r, scratch + 2 * kSlots, sizeof r, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
     cudaGetLastError();
-    return HEAT_ECUDA;
+    return heat::cuda_fail(e, "heat_norm_noalloc");
   }
   if (checksum) *checksum = r[0];
   if (l2) *l2 = std::sqrt(r[1]);

@@ -22,7 +22,7 @@ namespace tma {
 namespace {
 
 constexpr unsigned kSuspendNs = 2000;      // try_wait suspend-time hint
-constexpr unsigned kWaitLimit = 1u << 22;  // bounded wait: attempts before giving up
+using heat::kWaitLimit;  // bounded wait: attempts before giving up (heat_internal.h)
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
   return (unsigned)__cvta_generic_to_shared(p);

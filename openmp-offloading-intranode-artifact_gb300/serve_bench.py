@@ -33,6 +33,56 @@ def log_uniform(rng: random.Random, lo: float, hi: float) -> float:
     return math.exp(rng.uniform(math.log(lo), math.log(hi)))
 
 
+def run(requests: int = 10000, rate: float = 200.0, budget_gb: float = 160.0, tick: int = 32,
+        prep_threads: int = 4, seed: int = 4, min_axis: int = 32, max_axis: int = 512,
+        min_steps: int = 50, max_steps: int = 5000, device: int = 0) -> dict:
+    """Serve one Poisson request stream of configuration 4; returns the JSON record."""
+    rng = random.Random(seed)
+    reqs, t = [], 0.0
+    for q in range(requests):
+        t += rng.expovariate(rate)
+        nx, ny, nz = (int(round(log_uniform(rng, min_axis, max_axis))) for _ in range(3))
+        steps = int(round(log_uniform(rng, min_steps, max_steps)))
+        reqs.append((t, nx, ny, nz, steps, H.HEAT_FP64 if rng.random() < 0.5 else H.HEAT_FP32C,
+                     1_000_000 * seed + q))
+    offered = sum((r[1] - 2) * (r[2] - 2) * (r[3] - 2) * r[4] for r in reqs)
+    span = reqs[-1][0] if reqs else 0.0
+
+    srv = H.Server(budget_bytes=int(budget_gb * (1 << 30)), tick_steps=tick,
+                   prep_threads=prep_threads)
+    with ClockSampler(device) as clk:
+        t0 = time.perf_counter()
+        for (ta, nx, ny, nz, steps, prec, sd) in reqs:
+            delay = ta - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            srv.submit(nx, ny, nz, steps, precision=prec, cfg=0, seed=sd)
+        srv.wait_idle()
+        wall = time.perf_counter() - t0
+    res = srv.poll(max_results=requests + 16)
+    st = srv.stats()
+    srv.close()
+    lat64 = sorted(x["done_ms"] - x["submit_ms"] for x, r in zip(sorted(res, key=lambda x: x["id"]), reqs)
+                   if r[5] == H.HEAT_FP64 and x["status"] == 0)
+    lat32 = sorted(x["done_ms"] - x["submit_ms"] for x, r in zip(sorted(res, key=lambda x: x["id"]), reqs)
+                   if r[5] == H.HEAT_FP32C and x["status"] == 0)
+    pct = lambda v, p: v[min(len(v) - 1, int(round(p * (len(v) - 1))))] if v else None
+    return {"workload": f"config4: {requests} requests, Poisson {rate}/s, axes log-U[{min_axis},"
+                        f"{max_axis}], steps log-U[{min_steps},{max_steps}], 50/50 FP64/FP32C, "
+                        f"budget {budget_gb} GB, tick {tick}",
+            "offered_updates": offered, "arrival_span_s": round(span, 2),
+            "offered_glups": round(offered / span / 1e9, 1) if span > 0 else None,
+            "wall_s": round(wall, 2), "p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
+            "mean_ms": round(st["mean_ms"], 2), "max_ms": round(st["max_ms"], 2),
+            "p50_ms_fp64": pct(lat64, 0.5), "p99_ms_fp64": pct(lat64, 0.99),
+            "p50_ms_fp32c": pct(lat32, 0.5), "p99_ms_fp32c": pct(lat32, 0.99),
+            "glups": round(st["glups"], 2), "completed": st["completed"], "rejected": st["rejected"],
+            "peak_gb": round(st["peak_bytes"] / (1 << 30), 2), "batch_steps": st["batch_steps"],
+            "kernel_launches": st["kernel_launches"],
+            "gpu_busy_frac": round(st["gpu_ms"] * 1e-3 / wall, 3) if wall > 0 else None,
+            "clocks": clk.summary()}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--requests", type=int, default=10000)
@@ -46,51 +96,8 @@ def main() -> None:
     ap.add_argument("--min-steps", type=int, default=50)
     ap.add_argument("--max-steps", type=int, default=5000)
     a = ap.parse_args()
-
-    rng = random.Random(a.seed)
-    reqs, t = [], 0.0
-    for q in range(a.requests):
-        t += rng.expovariate(a.rate)
-        nx, ny, nz = (int(round(log_uniform(rng, a.min_axis, a.max_axis))) for _ in range(3))
-        steps = int(round(log_uniform(rng, a.min_steps, a.max_steps)))
-        reqs.append((t, nx, ny, nz, steps, H.HEAT_FP64 if rng.random() < 0.5 else H.HEAT_FP32C,
-                     1_000_000 * a.seed + q))
-    offered = sum((r[1] - 2) * (r[2] - 2) * (r[3] - 2) * r[4] for r in reqs)
-    span = reqs[-1][0] if reqs else 0.0
-
-    srv = H.Server(budget_bytes=int(a.budget_gb * (1 << 30)), tick_steps=a.tick,
-                   prep_threads=a.prep_threads)
-    with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        for (ta, nx, ny, nz, steps, prec, seed) in reqs:
-            delay = ta - (time.perf_counter() - t0)
-            if delay > 0:
-                time.sleep(delay)
-            srv.submit(nx, ny, nz, steps, precision=prec, cfg=0, seed=seed)
-        srv.wait_idle()
-        wall = time.perf_counter() - t0
-    res = srv.poll(max_results=a.requests + 16)
-    st = srv.stats()
-    srv.close()
-    lat64 = sorted(x["done_ms"] - x["submit_ms"] for x, r in zip(sorted(res, key=lambda x: x["id"]), reqs)
-                   if r[5] == H.HEAT_FP64 and x["status"] == 0)
-    lat32 = sorted(x["done_ms"] - x["submit_ms"] for x, r in zip(sorted(res, key=lambda x: x["id"]), reqs)
-                   if r[5] == H.HEAT_FP32C and x["status"] == 0)
-    pct = lambda v, p: v[min(len(v) - 1, int(round(p * (len(v) - 1))))] if v else None
-    out = {"workload": f"config4: {a.requests} requests, Poisson {a.rate}/s, axes log-U[{a.min_axis},"
-                       f"{a.max_axis}], steps log-U[{a.min_steps},{a.max_steps}], 50/50 FP64/FP32C, "
-                       f"budget {a.budget_gb} GB, tick {a.tick}",
-           "offered_updates": offered, "arrival_span_s": round(span, 2),
-           "offered_glups": round(offered / span / 1e9, 1) if span > 0 else None,
-           "wall_s": round(wall, 2), "p50_ms": round(st["p50_ms"], 2), "p99_ms": round(st["p99_ms"], 2),
-           "mean_ms": round(st["mean_ms"], 2), "max_ms": round(st["max_ms"], 2),
-           "p50_ms_fp64": pct(lat64, 0.5), "p99_ms_fp64": pct(lat64, 0.99),
-           "p50_ms_fp32c": pct(lat32, 0.5), "p99_ms_fp32c": pct(lat32, 0.99),
-           "glups": round(st["glups"], 2), "completed": st["completed"], "rejected": st["rejected"],
-           "peak_gb": round(st["peak_bytes"] / (1 << 30), 2), "batch_steps": st["batch_steps"],
-           "kernel_launches": st["kernel_launches"],
-           "gpu_busy_frac": round(st["gpu_ms"] * 1e-3 / wall, 3) if wall > 0 else None,
-           "clocks": clk.summary()}
+    out = run(a.requests, a.rate, a.budget_gb, a.tick, a.prep_threads, a.seed, a.min_axis,
+              a.max_axis, a.min_steps, a.max_steps)
     print(json.dumps(out), flush=True)
 
 

@@ -3,7 +3,7 @@ reference's own result-reduction tools, to pin pipeline.py against them.
 
 Run here, where the reference tree is present (it is not on the GPU machine):
 
-    python tests/golden/make_pipeline_golden.py [/path/to/reference]
+    python tests/golden/make_pipeline_golden.py <reference checkout root>
 
 What it records:
 
@@ -101,7 +101,9 @@ def gamma_with_reference(ref: Path, summary_text: str, exe: str) -> str:
 
 
 def main() -> None:
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_pipeline_golden.py <reference checkout root>")
+    ref = Path(sys.argv[1])
     out = {"sets": {}, "gamma": {}, "own": {}}
     for key, rel in SETS.items():
         base = ref / rel

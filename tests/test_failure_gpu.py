@@ -3,6 +3,10 @@
   - a bounded device-side wait gives up: an mbarrier that nothing arrives at,
     waited on with the TMA kernels' own bounded wait (capped at a few
     milliseconds), returns HEAT_ETIMEOUT, and the device stays usable;
+  - the product FP32C two-step kernel, launched with its wait limit at 0
+    attempts, gives up, flags its context and returns; heat_sync, heat_norm,
+    heat_get_field and heat_batch_run each report HEAT_ETIMEOUT (once), the
+    context's field is untouched, and solves after it still match the oracle;
   - a context larger than the device returns HEAT_ENOMEM from its first device
     allocation (before any host data is read) and leaves nothing behind.
 """
@@ -56,3 +60,54 @@ def test_context_larger_than_the_device_returns_enomem(H, oracle, precision):
     assert st == H.HEAT_ENOMEM and not ctx.value
     assert b"bytes" in H.lib().heat_strerror(st)
     assert small_solve_matches_oracle(H, oracle)
+
+
+def fp32c_ctx(H):
+    kappa, u0, h, dt = H.inputs_config(0, 7, 40, 36, 30)
+    return H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C), (kappa, u0, h, dt)
+
+
+def test_product_kernel_timeout_reaches_every_sync_point(H, oracle):
+    s, (kappa, u0, h, dt) = fp32c_ctx(H)
+    with s:
+        s.step(4)
+        before = s.field()
+        lib = H.lib()
+        # heat_sync reports it, once
+        assert lib.heat_diag_fp32c_timeout(s._ctx) == H.HEAT_OK
+        assert lib.heat_sync(s._ctx) == H.HEAT_ETIMEOUT
+        assert lib.heat_sync(s._ctx) == H.HEAT_OK
+        # heat_norm
+        assert lib.heat_diag_fp32c_timeout(s._ctx) == H.HEAT_OK
+        l2, cs = C.c_double(), C.c_double()
+        assert lib.heat_norm(s._ctx, C.byref(l2), C.byref(cs)) == H.HEAT_ETIMEOUT
+        # heat_get_field: the copy is made, the status says the launch gave up
+        assert lib.heat_diag_fp32c_timeout(s._ctx) == H.HEAT_OK
+        out = np.empty_like(before)
+        assert lib.heat_get_field(s._ctx, out.ctypes.data) == H.HEAT_ETIMEOUT
+        assert bits_equal(out, before)  # the failed launch wrote nothing
+        assert s.stats()[0] == 4
+        # heat_batch_run of a batch holding the context
+        assert lib.heat_diag_fp32c_timeout(s._ctx) == H.HEAT_OK
+        with H.Batch() as b:
+            b.add(s, 2)
+            n = C.c_longlong()
+            assert lib.heat_batch_run(b._b, -1, C.byref(n)) == H.HEAT_ETIMEOUT
+            assert n.value == 2
+            b.remove(s)
+        s.sync()
+        # the context keeps working: its next steps equal a fresh context's
+        s.step(2)
+        got = s.field()
+    with H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C) as ref:
+        ref.step(8)
+        assert bits_equal(got, ref.field())
+    assert small_solve_matches_oracle(H, oracle)
+
+
+def test_product_kernel_timeout_needs_the_two_step_form(H):
+    kappa, u0, h, dt = H.inputs_config(0, 7, 20, 18, 16)
+    with H.Solver(kappa, u0, h, dt) as s:
+        assert H.lib().heat_diag_fp32c_timeout(s._ctx) == H.HEAT_ESTATE
+    with H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C, flags=H.HEAT_NO_TEMPORAL) as s:
+        assert H.lib().heat_diag_fp32c_timeout(s._ctx) == H.HEAT_ESTATE
