@@ -168,13 +168,28 @@ int heat_batch_stats(heat_batch *b, long long *kernel_launches, long long *graph
                      long long *batch_steps);
 int heat_batch_destroy(heat_batch *b);
 
-/* Autotune the batch kernel's z-chunk for one form (precision + HEAT_BITEXACT
- * / HEAT_HWFP64 flags) over the size classes up to max_nz (<= 0: all), and
- * write the JSON cache ($HEAT_TUNE_CACHE, else heat_tune.json beside the
- * library).  Classes already cached are kept unless force != 0.              */
+/* Autotune the batch table kernels for one form (precision + HEAT_BITEXACT /
+ * HEAT_HWFP64 flags) over the size classes (grid depth nz <= 64, 128, 256,
+ * 384, 512, 1024, 2048, larger) up to max_nz (<= 0: all), and write the JSON
+ * cache ($HEAT_TUNE_CACHE, else heat_tune.json beside the library; read again
+ * when that path changes).  Per class it picks, by timing a GPU-filling batch
+ * of that class, the z-chunk, the rows per thread, the blocks-per-SM variant
+ * and, for HEAT_FP32C, the temporal depth (heat_tune_entry).  Classes already
+ * cached are kept unless force != 0.  No counterpart in the reference, whose
+ * launch shape is a fixed dim3 block(8,8,8) (1-cuda.cu:123-128).            */
 int heat_tune_batch(int precision, unsigned flags, int max_nz, int force);
 /* z-chunk the batch kernel will use for a grid of depth nz.                   */
 int heat_tune_lookup(int precision, unsigned flags, int nz, int *kchunk);
+
+/* Every choice the batch makes for a grid of depth nz of this form.         */
+typedef struct heat_tune_entry {
+  int kchunk;          /* planes per tile's z-walk                          */
+  int rows;            /* rows per thread: tiles of 32 x (8 * rows) columns  */
+  int blocks_per_sm;   /* table kernel variant: 2, 3 or 4 resident blocks    */
+  int depth;           /* time steps per launch: 1, or 2 (HEAT_FP32C grids
+                          without a source term, 32 x 16 TMA-staged tiles)   */
+} heat_tune_entry;
+int heat_tune_choice(int precision, unsigned flags, int nz, heat_tune_entry *out);
 
 /* ---- continuous-batching solve server ------------------------------------ */
 

@@ -426,6 +426,11 @@ cudaError_t enqueue_ctx_steps(heat_ctx *c, int cur, long long n, cudaStream_t st
   return e;
 }
 
+cudaError_t enqueue_one_step(heat_ctx *c, int cur, cudaStream_t st, long long *launches) {
+  if (launches) ++*launches;
+  return enqueue_one(c, cur, st);
+}
+
 int ctx_flips(const heat_ctx *c, long long n) {
   return (int)((two_step_form(c) ? n / 2 + n % 2 : n) & 1);
 }

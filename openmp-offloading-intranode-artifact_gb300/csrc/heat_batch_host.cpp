@@ -39,13 +39,14 @@ struct heat_batch {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   unsigned flags = 0;
-  int kchunk_override = 0;
+  heat::TuneChoice override_ = {0, 0, 0, 0};  // fields > 0 replace the tuned choices
 
   struct Entry {
     heat_ctx *ctx;
     long long remaining;
     long long base_steps;  // ctx->steps_done when the table was built
     bool solo;             // stepped with its single-grid kernels
+    bool pairs;            // in the table with two steps per launch (FP32C, depth 2)
   };
   std::vector<Entry> entries;
   std::vector<int> active;  // entry indices in table order, then solo entries
@@ -60,6 +61,10 @@ struct heat_batch {
   size_t g_cap[2] = {0, 0};
   heat::BatchTile *t_buf[2] = {nullptr, nullptr};
   size_t t_cap[2] = {0, 0};
+  CUtensorMap *m_buf[2] = {nullptr, nullptr};  // two-step tiles' tensor maps, 7 per grid
+  size_t m_cap[2] = {0, 0};
+  std::vector<int> pairs;       // active entries in the table with two steps per launch
+  long long pair_flips = 0;     // buffer swaps of those grids since the table was built
   cudaEvent_t table_ev[2] = {nullptr, nullptr};
   bool table_used[2] = {false, false};
   // Table uploads run on their own stream (a pageable upload first waits for
@@ -102,11 +107,11 @@ int batch_form(const heat_ctx *c) {
   if (c->flags & HEAT_NAIVE) return -1;
   if (c->flags & HEAT_BITEXACT) return kFormExact;
   if (!c->kq) return kFormHw;
-  return (c->hw_rows == 4 && !c->rhs && batch_ws_usable()) ? kFormMixWs : kFormMix;
+  return (c->hw_rows == 4 && !c->rhs && batch_ws_usable(4)) ? kFormMixWs : kFormMix;
 }
 
-void batch_set_kchunk_override(heat_batch *b, int kchunk) {
-  b->kchunk_override = kchunk;
+void batch_set_override(heat_batch *b, const TuneChoice &ch) {
+  b->override_ = ch;
   b->dirty = true;
 }
 
@@ -152,6 +157,7 @@ void release(heat_batch *b) {
   for (int i = 0; i < 2; ++i) {
     if (b->g_buf[i]) cudaFree(b->g_buf[i]);
     if (b->t_buf[i]) cudaFree(b->t_buf[i]);
+    if (b->m_buf[i]) cudaFree(b->m_buf[i]);
     if (b->table_ev[i]) cudaEventDestroy(b->table_ev[i]);
   }
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
@@ -188,7 +194,8 @@ heat::BatchGrid describe(const heat_ctx *c, int form) {
   g.factor = c->factor;
   g.cur = c->cur;
   g.hw_rows = c->hw_rows;
-  if (form == heat::kFormF32c) {
+  g.err = c->err;
+  if (form == heat::kFormF32c || form == heat::kFormF32c2) {
     g.f[0] = c->v[0];
     g.f[1] = c->v[1];
     g.cr[0] = c->carry[0];
@@ -213,41 +220,78 @@ heat::BatchGrid describe(const heat_ctx *c, int form) {
 
 // Throughput guesses (GLUP/s on GB300) used only to split the SMs between
 // forms that run side by side.
-const double kFormRate[heat::kNumForms] = {100.0, 80.0, 29.0, 200.0, 110.0};
+const double kFormRate[heat::kNumForms] = {100.0, 80.0, 29.0, 200.0, 110.0, 300.0};
+
+// A side stream (and its join event) for kind f, created on first use.
+bool ensure_side(heat_batch *b, int f) {
+  if (b->side[f]) return true;
+  if (cudaStreamCreateWithFlags(&b->side[f], cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join_ev[f], cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return true;
+}
 
 int rebuild(heat_batch *b) {
   drop_graph(b);
   b->active.clear();
   b->solo.clear();
+  b->pairs.clear();
+  b->pair_flips = 0;
   std::vector<heat::BatchGrid> grids;
   std::vector<heat::BatchTile> per_form[heat::kNumKinds];
+  std::vector<CUtensorMap> maps;      // the two-step grids' maps, 7 each
+  std::vector<std::pair<int, int>> map_at;  // (grid index, first map)
   double work[heat::kNumKinds] = {};
   for (size_t e = 0; e < b->entries.size(); ++e) {
     heat_batch::Entry &en = b->entries[e];
     if (en.remaining <= 0) continue;
-    const heat_ctx *c = en.ctx;
+    heat_ctx *c = en.ctx;
     en.base_steps = c->steps_done;
+    en.pairs = false;
     const long long pts = (long long)(c->g.nx - 2) * (c->g.ny - 2) * (c->g.nz - 2);
     en.solo = b->solo_points > 0 && pts >= b->solo_points;
     if (en.solo) {
       b->solo.push_back((int)e);
       continue;
     }
-    const int form = heat::batch_form(c);
-    const int kind = 2 * form + (grid_has_rhs(c) ? 1 : 0);
+    int form = heat::batch_form(c);
+    // The autotuner's choices for the grid's form and depth class (the
+    // warpgroup-split form shares the hybrid form's entries).
+    const int tform = form == heat::kFormMixWs ? heat::kFormMix : form;
+    heat::TuneChoice ch = heat::tuned_choice(tform, c->g.nz);
+    if (b->override_.kchunk > 0) ch.kchunk = b->override_.kchunk;
+    if (b->override_.rows > 0) ch.rows = b->override_.rows;
+    if (b->override_.minb > 0) ch.minb = b->override_.minb;
+    if (b->override_.depth > 0) ch.depth = b->override_.depth;
+    const int minb = std::max(heat::kMinbLo, std::min(ch.minb, heat::kMinbLo + heat::kNumMinb - 1));
+    if (form == heat::kFormF32c && ch.depth == 2 && heat::two_step_form(c)) form = heat::kFormF32c2;
+    if (form == heat::kFormMixWs && !heat::batch_ws_usable(minb)) form = heat::kFormMix;
+    const int kind = heat::kind_of(form, grid_has_rhs(c), form == heat::kFormF32c2 ? heat::kMinbLo : minb);
     const int gi = (int)grids.size();
     grids.push_back(describe(c, form));
     b->active.push_back((int)e);
     const int interior = c->g.nz - 2;
-    // the warpgroup-split form walks tiles as the hybrid one does: same z-chunk
-    const int tform = form == heat::kFormMixWs ? heat::kFormMix : form;
-    int kc = b->kchunk_override > 0 ? b->kchunk_override : heat::tuned_kchunk(tform, c->g.nz);
-    kc = std::max(1, std::min(kc, interior));
-    const int ntx = (c->g.nx - 2 + 31) / 32, nty = (c->g.ny - 2 + 7) / 8;
+    int kc = std::max(1, std::min(ch.kchunk, interior));
+    int rows = std::max(1, std::min(ch.rows, 2)), tile_h = 8 * rows;
+    if (form == heat::kFormF32c2) {
+      en.pairs = true;
+      b->pairs.push_back((int)e);
+      map_at.push_back({gi, (int)maps.size()});
+      maps.resize(maps.size() + 7);
+      if (!heat::encode_fp32c_maps(&maps[maps.size() - 7], c->v, c->carry, c->fcf, c->g))
+        return HEAT_ECUDA;
+      // two steps per 32 x 16 tile; the temporal blocking wants long z-walks
+      kc = std::max(kc, std::min(16, interior));
+      rows = 1;
+      tile_h = 16;
+    }
+    const int ntx = (c->g.nx - 2 + 31) / 32, nty = (c->g.ny - 2 + tile_h - 1) / tile_h;
     for (int k0 = 1; k0 < c->g.nz - 1; k0 += kc) {
       const int k1 = std::min(k0 + kc, c->g.nz - 1);
       for (int ty = 0; ty < nty; ++ty)
-        for (int tx = 0; tx < ntx; ++tx) per_form[kind].push_back({gi, tx, ty, k0, k1});
+        for (int tx = 0; tx < ntx; ++tx) per_form[kind].push_back({gi, tx, ty, k0, k1, rows});
     }
     work[kind] += (double)(c->g.nx - 2) * (c->g.ny - 2) * interior / kFormRate[form];
   }
@@ -288,7 +332,16 @@ int rebuild(heat_batch *b) {
   }
   int rc = grow(&b->g_buf[nb], &b->g_cap[nb], std::max<size_t>(1, grids.size()));
   if (rc == HEAT_OK) rc = grow(&b->t_buf[nb], &b->t_cap[nb], std::max<size_t>(1, tiles.size()));
+  if (rc == HEAT_OK && !maps.empty()) rc = grow(&b->m_buf[nb], &b->m_cap[nb], maps.size());
   if (rc != HEAT_OK) return rc;
+  for (const auto &gm : map_at) grids[gm.first].tmaps = b->m_buf[nb] + gm.second;
+  for (int f = 0; f < heat::kNumKinds; ++f)
+    if (b->tile_count[f] && !ensure_side(b, f)) return HEAT_ECUDA;
+  if (!maps.empty() && cudaMemcpyAsync(b->m_buf[nb], maps.data(), maps.size() * sizeof(CUtensorMap),
+                                       cudaMemcpyHostToDevice, b->copy_stream) != cudaSuccess) {
+    cudaGetLastError();
+    return HEAT_ECUDA;
+  }
   // Pageable sources: the copies are staged before the calls return.
   if (!grids.empty() &&
       (cudaMemcpyAsync(b->g_buf[nb], grids.data(), grids.size() * sizeof(heat::BatchGrid),
@@ -314,9 +367,10 @@ void advance(heat_batch *b, long long n) {
   for (int e : b->active) {
     heat_batch::Entry &en = b->entries[e];
     en.ctx->steps_done += n;
-    if (en.solo ? heat::ctx_flips(en.ctx, n) : (n & 1)) en.ctx->cur ^= 1;
+    if ((en.solo || en.pairs) ? heat::ctx_flips(en.ctx, n) : (n & 1)) en.ctx->cur ^= 1;
     en.remaining -= n;
   }
+  b->pair_flips += n / 2 + n % 2;
   b->since_build += n;
   b->batch_steps += n;
 }
@@ -331,21 +385,44 @@ cudaError_t enqueue_solo(heat_batch *b, int n, cudaStream_t st, long long *launc
   return err;
 }
 
-// Enqueue `n` steps starting at parity p: each form's kernel on its own side
-// stream (forked from and joined back to the batch stream) when several forms
-// are present, so a memory-bound and a compute-bound form share the SMs; the
-// solo grids on a further side stream.  *launches counts the kernels.
+// n steps of one kind's tiles on stream st: one launch per step with the step
+// parity (p + s) for single-step kinds; for the two-step FP32C kind, n / 2
+// two-step launches (each swapping the grids' buffers once, counted from
+// pair_flips) and, for an odd n, one single step of each such grid with its
+// single-grid kernel.
+cudaError_t enqueue_kind(heat_batch *b, int f, int p, int n, cudaStream_t st,
+                         long long *launches) {
+  cudaError_t err = cudaSuccess;
+  if (heat::form_of_kind(f) != heat::kFormF32c2) {
+    for (int s = 0; s < n && err == cudaSuccess; ++s)
+      err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
+                               (p + s) & 1, b->form_blocks[f], st);
+    *launches += n;
+    return err;
+  }
+  for (int s = 0; s < n / 2 && err == cudaSuccess; ++s) {
+    err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
+                             (int)((b->pair_flips + s) & 1), b->form_blocks[f], st);
+    *launches += 1;
+  }
+  if (n & 1)
+    for (size_t a = 0; a < b->pairs.size() && err == cudaSuccess; ++a) {
+      heat_ctx *c = b->entries[b->pairs[a]].ctx;
+      err = heat::enqueue_one_step(c, c->cur ^ ((n / 2) & 1), st, launches);
+    }
+  return err;
+}
+
+// Enqueue `n` steps starting at parity p: each kind's kernel on its own side
+// stream (forked from and joined to the batch stream) when several are
+// present, so a memory-bound and a compute-bound form share the SMs; the solo
+// grids on a further side stream.  *launches counts the kernels.
 cudaError_t enqueue_steps(heat_batch *b, int p, int n, long long *launches) {
   cudaError_t err = cudaSuccess;
   const int parts = b->nforms + (b->solo.empty() ? 0 : 1);
   if (parts <= 1 || !b->concurrent) {
-    for (int f = 0; f < heat::kNumKinds; ++f) {
-      if (!b->tile_count[f]) continue;
-      for (int s = 0; s < n && err == cudaSuccess; ++s)
-        err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
-                                 (p + s) & 1, b->form_blocks[f], b->stream);
-      *launches += n;
-    }
+    for (int f = 0; f < heat::kNumKinds && err == cudaSuccess; ++f)
+      if (b->tile_count[f]) err = enqueue_kind(b, f, p, n, b->stream, launches);
     if (err == cudaSuccess) err = enqueue_solo(b, n, b->stream, launches);
     return err;
   }
@@ -359,10 +436,7 @@ cudaError_t enqueue_steps(heat_batch *b, int p, int n, long long *launches) {
   for (int f = 0; f < heat::kNumKinds && err == cudaSuccess; ++f) {
     if (!b->tile_count[f]) continue;
     err = cudaStreamWaitEvent(b->side[f], b->fork_ev, 0);
-    for (int s = 0; s < n && err == cudaSuccess; ++s)
-      err = heat::launch_batch(f, b->d_grids, b->d_tiles + b->tile_begin[f], b->tile_count[f],
-                               (p + s) & 1, b->form_blocks[f], b->side[f]);
-    *launches += n;
+    if (err == cudaSuccess) err = enqueue_kind(b, f, p, n, b->side[f], launches);
     if (err == cudaSuccess) err = cudaEventRecord(b->join_ev[f], b->side[f]);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(b->stream, b->join_ev[f], 0);
   }
@@ -440,9 +514,6 @@ int heat_batch_create(heat_batch **out, void *stream, unsigned flags) {
             cudaEventCreateWithFlags(&b->table_ev[1], cudaEventDisableTiming) == cudaSuccess &&
             cudaEventCreateWithFlags(&b->copy_ev, cudaEventDisableTiming) == cudaSuccess &&
             cudaStreamCreateWithFlags(&b->copy_stream, cudaStreamNonBlocking) == cudaSuccess;
-  for (int f = 0; f < heat::kNumKinds && ok; ++f)
-    ok = cudaStreamCreateWithFlags(&b->side[f], cudaStreamNonBlocking) == cudaSuccess &&
-         cudaEventCreateWithFlags(&b->join_ev[f], cudaEventDisableTiming) == cudaSuccess;
   ok = ok && cudaStreamCreateWithFlags(&b->solo_stream, cudaStreamNonBlocking) == cudaSuccess &&
        cudaEventCreateWithFlags(&b->solo_join, cudaEventDisableTiming) == cudaSuccess;
   if (const char *ev = std::getenv("HEAT_BATCH_SOLO_POINTS")) b->solo_points = std::atoll(ev);

@@ -30,6 +30,7 @@
 
 #include <cuda.h>
 
+#include "heat_batch_internal.h"
 #include "heat_internal.h"
 #include "heat_tma.cuh"
 #include "heat_walk.cuh"
@@ -84,17 +85,20 @@ struct Maps {
   CUtensorMap v, c, wx, wy, wz;
 };
 
-__global__ void __launch_bounds__(NT, 2)
-    k_fp32c_tb2(const __grid_constant__ Maps in, float *__restrict__ vn,
-                uint16_t *__restrict__ cn, int nx, int ny, int nz, int P, size_t S, int kchunk,
-                int *__restrict__ err, unsigned wait_limit) {
+// Two steps over one (32 x 16)-column tile with origin (x0, y0), planes
+// [kb, ke), of a field whose five input arrays the tensor maps v, c, wx, wy,
+// wz describe (in kernel parameters for a single grid; in device memory for
+// the batch table).  Writes vn / cn.  Returns true when a bounded wait ran out
+// (after its own loads in flight have landed).
+__device__ __forceinline__ bool tb2_tile(const CUtensorMap *map_v, const CUtensorMap *map_c,
+                                         const CUtensorMap *map_wx, const CUtensorMap *map_wy,
+                                         const CUtensorMap *map_wz, float *__restrict__ vn,
+                                         uint16_t *__restrict__ cn, int x0, int y0, int nx,
+                                         int ny, int nz, int P, size_t S, int kb, int ke,
+                                         unsigned wait_limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x;
-  const int x0 = 1 + OX * blockIdx.x, y0 = 1 + OY * blockIdx.y;
-  const int kb = 1 + blockIdx.z * kchunk;
-  const int ke = min(kb + kchunk, nz - 1);
-  if (kb >= ke) return;
   const int X0 = x0 - 5, X0c = x0 - 9, Y0 = y0 - 2;  // box origins (X0 % 4 == 0, X0c % 8 == 0)
   const int pmin = max(kb - 2, 0), pmax = min(ke + 1, nz - 1);
 
@@ -120,11 +124,11 @@ __global__ void __launch_bounds__(NT, 2)
     unsigned long long *b = &sm.bar[s];
     tma::fence_proxy_async();
     mbar_expect(b, kSlotBytes);
-    tma_load3(sl.v, &in.v, X0, Y0, p, b);
-    tma_load3(sl.wx, &in.wx, X0, Y0, p, b);
-    tma_load3(sl.wy, &in.wy, X0, Y0, p, b);
-    tma_load3(sl.wz, &in.wz, X0, Y0, p, b);
-    tma_load3(sl.c, &in.c, X0c, Y0, p, b);
+    tma_load3(sl.v, map_v, X0, Y0, p, b);
+    tma_load3(sl.wx, map_wx, X0, Y0, p, b);
+    tma_load3(sl.wy, map_wy, X0, Y0, p, b);
+    tma_load3(sl.wz, map_wz, X0, Y0, p, b);
+    tma_load3(sl.c, map_c, X0c, Y0, p, b);
   };
   auto wait_plane = [&](int p) {
     if (!waiter || p < pmin || p > pmax || failed) return;
@@ -286,14 +290,49 @@ __global__ void __launch_bounds__(NT, 2)
     ib = ic;
     ic = t3;
   }
-  if (failed) {
-    if (tid == 0) atomicExch(err, 1);
+  if (failed && waiter) {
     // Let the block's own loads in flight land before its shared memory goes
     // (each wait bounded).
-    if (waiter)
-      for (int s = 0; s < R; ++s)
-        if (pending & (1u << s)) mbar_wait(&sm.bar[s], (phase >> s) & 1u);
+    for (int s = 0; s < R; ++s)
+      if (pending & (1u << s)) mbar_wait(&sm.bar[s], (phase >> s) & 1u);
   }
+  return failed;
+}
+
+__global__ void __launch_bounds__(NT, 2)
+    k_fp32c_tb2(const __grid_constant__ Maps in, float *__restrict__ vn,
+                uint16_t *__restrict__ cn, int nx, int ny, int nz, int P, size_t S, int kchunk,
+                int *__restrict__ err, unsigned wait_limit) {
+  const int kb = 1 + blockIdx.z * kchunk;
+  const int ke = min(kb + kchunk, nz - 1);
+  if (kb >= ke) return;
+  if (tb2_tile(&in.v, &in.c, &in.wx, &in.wy, &in.wz, vn, cn, 1 + OX * blockIdx.x,
+               1 + OY * blockIdx.y, nx, ny, nz, P, S, kb, ke, wait_limit) &&
+      threadIdx.x == 0)
+    atomicExch(err, 1);
+}
+
+// The batch table's two-step FP32C tiles: one block per tile, hardware
+// scheduled.  Grid g's maps are in device memory, seven per grid: v and carry
+// of buffers 0 and 1, then wx, wy, wz; each launch reads buffer cur ^ flip.
+__global__ void __launch_bounds__(NT, 2)
+    k_batch_fp32c_tb2(const BatchGrid *__restrict__ grids, const BatchTile *__restrict__ tiles,
+                      int flip) {
+  const BatchTile tl = tiles[blockIdx.x];
+  const BatchGrid &g = grids[tl.grid];
+  const int src = g.cur ^ flip, dst = src ^ 1;
+  const CUtensorMap *tm = static_cast<const CUtensorMap *>(g.tmaps);
+  // The maps were written by a host copy before the launch; order the tensor
+  // proxy's reads of them after it.
+  if (threadIdx.x < 7)
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm + threadIdx.x)
+                 : "memory");
+  __syncthreads();
+  if (tb2_tile(&tm[src], &tm[2 + src], &tm[4], &tm[5], &tm[6], (float *)g.f[dst], g.cr[dst],
+               1 + OX * tl.tx, 1 + OY * tl.ty, g.nx, g.ny, g.nz, g.P, g.S, tl.k0, tl.k1,
+               kWaitLimit) &&
+      threadIdx.x == 0)
+    atomicExch(g.err, 1);
 }
 
 bool encode(CUtensorMap *m, const void *base, bool bf16, const heat_geom &g) {
@@ -305,6 +344,25 @@ bool encode(CUtensorMap *m, const void *base, bool bf16, const heat_geom &g) {
 }  // namespace
 
 size_t fp32c_tb2_smem() { return sizeof(Smem) + 128; }
+
+cudaError_t launch_batch_fp32c_tb2(const BatchGrid *grids, const BatchTile *tiles, int ntiles,
+                                   int flip, cudaStream_t st) {
+  if (ntiles <= 0) return cudaSuccess;
+  static bool attr =
+      cudaFuncSetAttribute(k_batch_fp32c_tb2, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)fp32c_tb2_smem()) == cudaSuccess;
+  if (!attr) return cudaErrorInvalidConfiguration;
+  k_batch_fp32c_tb2<<<ntiles, NT, fp32c_tb2_smem(), st>>>(grids, tiles, flip);
+  return cudaGetLastError();
+}
+
+bool encode_fp32c_maps(CUtensorMap *m7, float *const v[2], uint16_t *const c[2],
+                       float *const w[3], const heat_geom &g) {
+  return encode(&m7[0], v[0], false, g) && encode(&m7[1], v[1], false, g) &&
+         encode(&m7[2], c[0], true, g) && encode(&m7[3], c[1], true, g) &&
+         encode(&m7[4], w[0], false, g) && encode(&m7[5], w[1], false, g) &&
+         encode(&m7[6], w[2], false, g);
+}
 
 // Whether the two-step kernel can run this geometry: row and plane strides in
 // bytes must be multiples of 16 for TMA (pitch a multiple of 8 points).

@@ -125,6 +125,8 @@ cudaError_t launch_fast_tma(double *u_new, const double *u_old, const unsigned l
 cudaError_t enqueue_ctx_steps(heat_ctx *c, int cur, long long n, cudaStream_t st,
                               long long *launches);
 int ctx_flips(const heat_ctx *c, long long n);
+// One step of context c from buffer `cur` with its single-grid one-step kernel.
+cudaError_t enqueue_one_step(heat_ctx *c, int cur, cudaStream_t st, long long *launches);
 
 // heat_fp32c.cu
 cudaError_t launch_fp32c(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,

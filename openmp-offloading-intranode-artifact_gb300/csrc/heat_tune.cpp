@@ -1,17 +1,27 @@
-// Autotuner of the batched kernel's z-chunk, per precision form and size class,
+// Autotuner of the batched table kernels, per precision form and size class,
 // cached to a JSON file.
 //
 // Size classes are by grid depth nz (the z extent each tile column walks):
-// nz <= 64, 128, 256, 384, 512, 1024, 2048 and larger.  For a class the tuner
-// builds a batch that fills the GPU the way a real batch does: copies of one
-// synthetic grid of that depth (configuration-0 fields; x and y extents
-// min(nz, 384); enough copies for ~48M points, at most 64), runs it with each
-// candidate z-chunk (8 ... 512, and the whole depth) for 2 warm-up + 6 timed
-// steps (CUDA events, graphs off), and keeps the fastest.  Batches look their
-// grids' classes up in the cache; classes not tuned yet use 32 planes.
+// nz <= 64, 128, 256, 384, 512, 1024, 2048 and larger.  Per class the tuner
+// chooses
+//   kchunk : planes per tile's z-walk (8 ... 512, or the whole depth),
+//   rows   : rows each thread walks, 8 apart (tile height 8 x rows: 8 or 16),
+//   minb   : the table kernel compiled for 2, 3 or 4 resident blocks per SM
+//            (its register cap per thread: 128, 80 or 64),
+//   depth  : time steps per launch, 1, or 2 for FP32C grids (the two-step TMA
+//            kernel on 32 x 16 tiles),
+// one after another (coordinate descent from the defaults 32 / 1 / the form's
+// default / 1).  For a class it builds a batch that fills the GPU the way a
+// real batch does: copies of one synthetic grid of that depth
+// (configuration-0 fields; x and y extents min(nz, 384); enough copies for
+// ~48M points, at most 64), times each candidate for 2 warm-up + 6 timed steps
+// (CUDA events, graphs off), and keeps the fastest.  Batches look their grids'
+// classes up in the cache; classes not tuned yet use the defaults.
 //
-// Cache file: $HEAT_TUNE_CACHE, else heat_tune.json next to libheat.so.  One
-// entry per line:  {"form": F, "nz_max": N, "kchunk": K, "glups": G},
+// Cache file: $HEAT_TUNE_CACHE, else heat_tune.json next to libheat.so (read
+// again whenever that path changes).  One entry per line:
+//   {"form": F, "nz_max": N, "kchunk": K, "rows": R, "minb": M, "depth": D, "glups": G},
+// (entries written before rows / minb / depth existed read with the defaults).
 
 #include <dlfcn.h>
 
@@ -27,13 +37,14 @@
 #include "heat_batch_internal.h"
 
 namespace heat {
-void batch_set_kchunk_override(heat_batch *b, int kchunk);
+void batch_set_override(heat_batch *b, const TuneChoice &ch);
 }
 
 namespace {
 
 struct TuneEntry {
-  int form, nz_max, kchunk;
+  int form, nz_max;
+  heat::TuneChoice ch;
   double glups;
 };
 
@@ -43,6 +54,7 @@ constexpr int kDefaultKchunk = 32;
 std::mutex g_mu;
 std::vector<TuneEntry> g_table;
 bool g_loaded = false;
+std::string g_loaded_path;
 char g_device[256] = "";
 
 std::string cache_path() {
@@ -56,20 +68,42 @@ std::string cache_path() {
   return "heat_tune.json";
 }
 
+heat::TuneChoice default_choice(int form) {
+  return {kDefaultKchunk, 1, heat::default_minb(form), 1};
+}
+
 void load_locked() {
-  if (g_loaded) return;
+  const std::string path = cache_path();
+  if (g_loaded && path == g_loaded_path) return;
   g_loaded = true;
-  FILE *f = std::fopen(cache_path().c_str(), "r");
+  g_loaded_path = path;
+  g_table.clear();
+  FILE *f = std::fopen(path.c_str(), "r");
   if (!f) return;
   char line[512];
   while (std::fgets(line, sizeof line, f)) {
     const char *p = std::strstr(line, "{\"form\":");
     if (!p) continue;
     TuneEntry t{};
-    if (std::sscanf(p, "{\"form\": %d, \"nz_max\": %d, \"kchunk\": %d, \"glups\": %lf", &t.form,
-                    &t.nz_max, &t.kchunk, &t.glups) == 4 &&
-        t.kchunk > 0)
-      g_table.push_back(t);
+    int kc = 0;
+    if (std::sscanf(p, "{\"form\": %d, \"nz_max\": %d, \"kchunk\": %d", &t.form, &t.nz_max,
+                    &kc) != 3 ||
+        kc <= 0 || t.form < 0 || t.form >= heat::kNumForms)
+      continue;
+    t.ch = default_choice(t.form);
+    t.ch.kchunk = kc;
+    int v = 0;
+    if (const char *q = std::strstr(p, "\"rows\":"); q && std::sscanf(q, "\"rows\": %d", &v) == 1 &&
+        v >= 1 && v <= 2)
+      t.ch.rows = v;
+    if (const char *q = std::strstr(p, "\"minb\":"); q && std::sscanf(q, "\"minb\": %d", &v) == 1 &&
+        v >= heat::kMinbLo && v < heat::kMinbLo + heat::kNumMinb)
+      t.ch.minb = v;
+    if (const char *q = std::strstr(p, "\"depth\":");
+        q && std::sscanf(q, "\"depth\": %d", &v) == 1 && v >= 1 && v <= 2)
+      t.ch.depth = v;
+    if (const char *q = std::strstr(p, "\"glups\":")) std::sscanf(q, "\"glups\": %lf", &t.glups);
+    g_table.push_back(t);
   }
   std::fclose(f);
 }
@@ -80,11 +114,15 @@ int save_locked() {
   std::fprintf(f, "{\"device\": \"%s\", \"entries\": [\n", g_device);
   for (size_t i = 0; i < g_table.size(); ++i) {
     const TuneEntry &t = g_table[i];
-    std::fprintf(f, " {\"form\": %d, \"nz_max\": %d, \"kchunk\": %d, \"glups\": %.3f}%s\n", t.form,
-                 t.nz_max, t.kchunk, t.glups, i + 1 < g_table.size() ? "," : "");
+    std::fprintf(f,
+                 " {\"form\": %d, \"nz_max\": %d, \"kchunk\": %d, \"rows\": %d, \"minb\": %d, "
+                 "\"depth\": %d, \"glups\": %.3f}%s\n",
+                 t.form, t.nz_max, t.ch.kchunk, t.ch.rows, t.ch.minb, t.ch.depth, t.glups,
+                 i + 1 < g_table.size() ? "," : "");
   }
   std::fprintf(f, "]}\n");
   std::fclose(f);
+  g_loaded_path = cache_path();
   return HEAT_OK;
 }
 
@@ -101,9 +139,10 @@ int form_of(int precision, unsigned flags) {
   return heat::kFormMix;
 }
 
-// GLUP/s of a batch of identical grids at z-chunk kc.
-double time_candidate(std::vector<heat_ctx *> &cs, heat_batch *b, int kc, cudaStream_t st) {
-  heat::batch_set_kchunk_override(b, kc);
+// GLUP/s of a batch of identical grids with the choices ch.
+double time_candidate(std::vector<heat_ctx *> &cs, heat_batch *b, const heat::TuneChoice &ch,
+                      cudaStream_t st) {
+  heat::batch_set_override(b, ch);
   long long taken = 0;
   for (heat_ctx *c : cs)
     if (heat_batch_add(b, c, 2) != HEAT_OK) return -1;
@@ -132,13 +171,13 @@ double time_candidate(std::vector<heat_ctx *> &cs, heat_batch *b, int kc, cudaSt
 
 namespace heat {
 
-int tuned_kchunk(int form, int nz) {
+TuneChoice tuned_choice(int form, int nz) {
   std::lock_guard<std::mutex> lk(g_mu);
   load_locked();
   const int cls = class_of(nz);
   for (const TuneEntry &t : g_table)
-    if (t.form == form && t.nz_max == cls) return t.kchunk;
-  return kDefaultKchunk;
+    if (t.form == form && t.nz_max == cls) return t.ch;
+  return default_choice(form);
 }
 
 }  // namespace heat
@@ -197,17 +236,37 @@ extern "C" int heat_tune_batch(int precision, unsigned flags, int max_nz, int fo
     }
     heat_batch *b = nullptr;
     if (rc == HEAT_OK) rc = heat_batch_create(&b, st, HEAT_BATCH_NO_GRAPHS);
-    int best_k = kDefaultKchunk;
+    heat::TuneChoice best_ch = default_choice(form);
     double best = -1;
     if (rc == HEAT_OK) {
-      std::vector<int> cands = {8, 16, 32, 64, 128, 256, 512, nz - 2};
-      for (int kc : cands) {
-        if (kc > nz - 2) continue;
-        double g = time_candidate(cs, b, kc, st);
+      // one parameter at a time, each from the best choice so far
+      auto consider = [&](heat::TuneChoice ch) {
+        const double g = time_candidate(cs, b, ch, st);
         if (g > best) {
           best = g;
-          best_k = kc;
+          best_ch = ch;
         }
+      };
+      for (int kc : {8, 16, 32, 64, 128, 256, 512, nz - 2}) {
+        if (kc > nz - 2) continue;
+        heat::TuneChoice ch = best_ch;
+        ch.kchunk = kc;
+        consider(ch);
+      }
+      for (int rows : {1, 2}) {
+        heat::TuneChoice ch = best_ch;
+        ch.rows = rows;
+        if (rows != best_ch.rows) consider(ch);
+      }
+      for (int m = heat::kMinbLo; m < heat::kMinbLo + heat::kNumMinb; ++m) {
+        heat::TuneChoice ch = best_ch;
+        ch.minb = m;
+        if (m != best_ch.minb) consider(ch);
+      }
+      if (form == heat::kFormF32c) {
+        heat::TuneChoice ch = best_ch;
+        ch.depth = 2;
+        consider(ch);
       }
     }
     if (b) heat_batch_destroy(b);
@@ -221,7 +280,7 @@ extern "C" int heat_tune_batch(int precision, unsigned flags, int max_nz, int fo
     g_table.erase(std::remove_if(g_table.begin(), g_table.end(),
                                  [&](const TuneEntry &t) { return t.form == form && t.nz_max == cls; }),
                   g_table.end());
-    g_table.push_back({form, cls, best_k, best});
+    g_table.push_back({form, cls, best_ch, best});
   }
   cudaStreamDestroy(st);
   std::lock_guard<std::mutex> lk(g_mu);
@@ -231,6 +290,17 @@ extern "C" int heat_tune_batch(int precision, unsigned flags, int max_nz, int fo
 
 extern "C" int heat_tune_lookup(int precision, unsigned flags, int nz, int *kchunk) {
   if (!kchunk || nz < 3) return HEAT_EINVAL;
-  *kchunk = heat::tuned_kchunk(form_of(precision, flags), nz);
+  *kchunk = heat::tuned_choice(form_of(precision, flags), nz).kchunk;
+  return HEAT_OK;
+}
+
+extern "C" int heat_tune_choice(int precision, unsigned flags, int nz, heat_tune_entry *out) {
+  if (!out || nz < 3) return HEAT_EINVAL;
+  if (precision != HEAT_FP64 && precision != HEAT_FP32C) return HEAT_EINVAL;
+  const heat::TuneChoice ch = heat::tuned_choice(form_of(precision, flags), nz);
+  out->kchunk = ch.kchunk;
+  out->rows = ch.rows;
+  out->blocks_per_sm = ch.minb;
+  out->depth = ch.depth;
   return HEAT_OK;
 }

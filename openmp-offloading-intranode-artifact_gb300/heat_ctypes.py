@@ -70,6 +70,10 @@ class HeatResult(C.Structure):
                 ("updates", C.c_double)]
 
 
+class HeatTuneEntry(C.Structure):
+    _fields_ = [("kchunk", C.c_int), ("rows", C.c_int), ("blocks_per_sm", C.c_int), ("depth", C.c_int)]
+
+
 class HeatServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong), ("completed", C.c_longlong),
                 ("rejected", C.c_longlong), ("resident", C.c_longlong), ("queued", C.c_longlong),
@@ -106,6 +110,7 @@ SIGNATURES = {
     "heat_batch_destroy": (C.c_int, [C.c_void_p]),
     "heat_tune_batch": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.c_int]),
     "heat_tune_lookup": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.POINTER(C.c_int)]),
+    "heat_tune_choice": (C.c_int, [C.c_int, C.c_uint, C.c_int, C.POINTER(HeatTuneEntry)]),
     "heat_server_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t, C.c_int, C.c_int]),
     "heat_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "heat_server_poll": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
@@ -309,6 +314,13 @@ def tune_lookup(precision: int, flags: int, nz: int) -> int:
     k = C.c_int()
     check(lib().heat_tune_lookup(precision, flags, nz, C.byref(k)), "heat_tune_lookup")
     return k.value
+
+
+def tune_choice(precision: int, flags: int, nz: int) -> dict:
+    """The batch's choices for a grid of depth nz: kchunk, rows, blocks_per_sm, depth."""
+    e = HeatTuneEntry()
+    check(lib().heat_tune_choice(precision, flags, nz, C.byref(e)), "heat_tune_choice")
+    return {k: getattr(e, k) for k, _ in HeatTuneEntry._fields_}
 
 
 class Server:

@@ -122,14 +122,61 @@ def test_config3_like_batch(H):
 def test_tuner_cache(H, tmp_path, monkeypatch):
     cache = tmp_path / "tune.json"
     monkeypatch.setenv("HEAT_TUNE_CACHE", str(cache))
-    # the library reads the cache once per process: point it at a fresh file
-    # only for the tuning call's own writes, then parse what it wrote
     H.tune_batch(H.HEAT_FP32C, 0, max_nz=64, force=True)
-    text = cache.read_text()
-    doc = json.loads(text)
+    doc = json.loads(cache.read_text())
     ent = [e for e in doc["entries"] if e["form"] == 3 and e["nz_max"] == 64]
     assert ent and ent[0]["kchunk"] >= 1 and ent[0]["glups"] > 0
-    assert H.tune_lookup(H.HEAT_FP32C, 0, 40) == ent[0]["kchunk"]
+    e = ent[0]
+    assert e["rows"] in (1, 2) and e["minb"] in (2, 3, 4) and e["depth"] in (1, 2)
+    assert H.tune_lookup(H.HEAT_FP32C, 0, 40) == e["kchunk"]
+    assert H.tune_choice(H.HEAT_FP32C, 0, 40) == {"kchunk": e["kchunk"], "rows": e["rows"],
+                                                   "blocks_per_sm": e["minb"], "depth": e["depth"]}
+    # the default FP64 form as well (its own entries)
+    H.tune_batch(H.HEAT_FP64, 0, max_nz=64, force=True)
+    doc = json.loads(cache.read_text())
+    ent = [e for e in doc["entries"] if e["form"] == 0 and e["nz_max"] == 64]
+    assert ent and ent[0]["depth"] == 1
+    assert H.tune_choice(H.HEAT_FP64, 0, 64)["blocks_per_sm"] == ent[0]["minb"]
+
+
+def write_cache(path, kchunk, rows, minb, depth):
+    """A tuning cache with the same choices for every form and size class."""
+    lines = [f' {{"form": {f}, "nz_max": {c}, "kchunk": {kchunk}, "rows": {rows}, "minb": {minb}, '
+             f'"depth": {depth}, "glups": 1.0}}'
+             for f in range(6) for c in (64, 128, 256, 384)]
+    path.write_text('{"device": "test", "entries": [\n' + ",\n".join(lines) + "\n]}\n")
+
+
+@pytest.mark.parametrize("kchunk,rows,minb,depth", [(16, 2, 2, 2), (8, 1, 3, 1), (64, 2, 4, 2),
+                                                    (32, 1, 4, 1)])
+@pytest.mark.parametrize("graphs", [True, False])
+def test_tuned_variants_equal_alone(H, tmp_path, monkeypatch, kchunk, rows, minb, depth, graphs):
+    """Every choice the autotuner can make -- z-chunk, rows per thread,
+    blocks-per-SM variant, FP32C temporal depth 2 (the two-step TMA kernel on
+    the table's tiles) -- leaves each grid's result bit-identical to its result
+    alone, for every form, odd step counts and runs cut into uneven pieces."""
+    cache = tmp_path / "tune.json"
+    write_cache(cache, kchunk, rows, minb, depth)
+    monkeypatch.setenv("HEAT_TUNE_CACHE", str(cache))
+    assert H.tune_choice(H.HEAT_FP32C, 0, 40) == {"kchunk": kchunk, "rows": rows,
+                                                   "blocks_per_sm": minb, "depth": depth}
+    rng = random.Random(17 + kchunk)
+    specs = []
+    for idx, (_, prec, fl) in enumerate(FORMS * 2):
+        shape = tuple(rng.randint(12, 72) for _ in range(3))
+        specs.append((shape, 700 + idx, prec, fl, rng.choice([7, 16, 23, 40, 51])))
+    solvers = [make(H, sh, sd, p, f) for sh, sd, p, f, _ in specs]
+    with H.Batch(graphs=graphs) as b:
+        for s, spec in zip(solvers, specs):
+            b.add(s, spec[4])
+        total = 0
+        for piece in (5, 16, 1, 19, 2, 33, 100):
+            total += b.run(piece)
+        assert total == max(sp[4] for sp in specs)
+    for s, (sh, sd, p, f, n) in zip(solvers, specs):
+        assert bits_equal(s.field(), alone(H, sh, sd, p, f, n)), (sh, p, f, n)
+        assert s.stats()[0] == n
+        s.close()
 
 
 @pytest.mark.parametrize("graphs", [True, False])
