@@ -267,6 +267,15 @@ def our_arm(a):
 
     n, ts = a.n, a.time_steps
     kappa, u0, h, dt = H.inputs_config(CFG, SEED, n, n, n)
+    # The inputs live in pinned host memory from the start (the end-to-end
+    # leg copies from it; every leg reads the same arrays).
+    pk = torch.empty(kappa.shape, dtype=torch.float64, pin_memory=True)
+    pu = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
+    pout = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
+    pk.numpy()[...] = kappa
+    pu.numpy()[...] = u0
+    del kappa, u0
+    kappa, u0 = pk.numpy(), pu.numpy()
     stream = torch.cuda.Stream()
     fp64_peak = H.fp64_rate()
 
@@ -289,6 +298,31 @@ def our_arm(a):
     ms = ev0.elapsed_time(ev1)
     l2n, csum = s.norm()
     s.close()
+
+    # ---- end to end through the ABI from pinned host memory, timed per call
+    # (right after the device-timed leg, before any other context exists)
+    e2e_steps = max(1, min(a.steps, 3))
+    phase_names = ("heat_init", "heat_step", "heat_get_field", "heat_destroy")
+    phases = dict.fromkeys(phase_names, 0.0)
+    with ClockSampler(dev) as e2e_clk:
+        for i in range(e2e_steps + 1):   # first one is warm-up
+            barrier()
+            t = [time.perf_counter()]
+            e = H.Solver(pk.numpy(), pu.numpy(), h, dt, stream=stream.cuda_stream)
+            t.append(time.perf_counter())
+            e.step(ts)
+            e.sync()                      # steps done (heat_get_field would wait for them anyway)
+            t.append(time.perf_counter())
+            e.field(pout.numpy())
+            t.append(time.perf_counter())
+            e.close()
+            t.append(time.perf_counter())
+            if i > 0:
+                for nm, a0, a1 in zip(phase_names, t, t[1:]):
+                    phases[nm] += a1 - a0
+    e2e_t = sum(phases.values())
+    e2e_s = max_over_ranks(e2e_t / e2e_steps, dist, "cuda")
+    e2e_value = replica_value(updates(n, ts), world, e2e_s)
 
     # ---- FP32-compensated form on the same inputs (precision pattern):
     # rate by CUDA events, error against the default FP64 form at 100 and ts
@@ -316,36 +350,6 @@ def our_arm(a):
     value = replica_value(upd, world, t_max * 1e-3)
     launch_ms = ms / (a.steps * ts)
     achieved_gbs = updates(n, 1) * BYTES_PER_UPDATE / (launch_ms * 1e-3) / 1e9
-
-    # ---- end to end through the ABI from pinned host memory, timed per call
-    pk = torch.empty(kappa.shape, dtype=torch.float64, pin_memory=True)
-    pu = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
-    pout = torch.empty(u0.shape, dtype=torch.float64, pin_memory=True)
-    pk.numpy()[...] = kappa
-    pu.numpy()[...] = u0
-    del kappa, u0
-    e2e_steps = max(1, min(a.steps, 3))
-    phase_names = ("heat_init", "heat_step", "heat_get_field", "heat_destroy")
-    phases = dict.fromkeys(phase_names, 0.0)
-    with ClockSampler(dev) as e2e_clk:
-        for i in range(e2e_steps + 1):   # first one is warm-up
-            barrier()
-            t = [time.perf_counter()]
-            e = H.Solver(pk.numpy(), pu.numpy(), h, dt, stream=stream.cuda_stream)
-            t.append(time.perf_counter())
-            e.step(ts)
-            e.sync()                      # steps done (heat_get_field would wait for them anyway)
-            t.append(time.perf_counter())
-            e.field(pout.numpy())
-            t.append(time.perf_counter())
-            e.close()
-            t.append(time.perf_counter())
-            if i > 0:
-                for nm, a0, a1 in zip(phase_names, t, t[1:]):
-                    phases[nm] += a1 - a0
-    e2e_t = sum(phases.values())
-    e2e_s = max_over_ranks(e2e_t / e2e_steps, dist, "cuda")
-    e2e_value = replica_value(updates(n, ts), world, e2e_s)
 
     # ---- configuration 3 (batch) and configuration 4 (serving), bounded
     batch_out = serve_out = ref_gpu = None
