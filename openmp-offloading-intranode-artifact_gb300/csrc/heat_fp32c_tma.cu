@@ -85,17 +85,36 @@ struct Maps {
   CUtensorMap v, c, wx, wy, wz;
 };
 
+// Where a tile finds its five tensor maps: the single-grid kernel's
+// __grid_constant__ parameters, or seven maps per grid in device memory for
+// the batch table (buffer `src` of v and carry, then wx, wy, wz).
+struct ParamMaps {
+  const Maps &in;
+  __device__ __forceinline__ const CUtensorMap *v() const { return &in.v; }
+  __device__ __forceinline__ const CUtensorMap *c() const { return &in.c; }
+  __device__ __forceinline__ const CUtensorMap *wx() const { return &in.wx; }
+  __device__ __forceinline__ const CUtensorMap *wy() const { return &in.wy; }
+  __device__ __forceinline__ const CUtensorMap *wz() const { return &in.wz; }
+};
+struct TableMaps {
+  const CUtensorMap *tm;
+  int src;
+  __device__ __forceinline__ const CUtensorMap *v() const { return &tm[src]; }
+  __device__ __forceinline__ const CUtensorMap *c() const { return &tm[2 + src]; }
+  __device__ __forceinline__ const CUtensorMap *wx() const { return &tm[4]; }
+  __device__ __forceinline__ const CUtensorMap *wy() const { return &tm[5]; }
+  __device__ __forceinline__ const CUtensorMap *wz() const { return &tm[6]; }
+};
+
 // Two steps over one (32 x 16)-column tile with origin (x0, y0), planes
-// [kb, ke), of a field whose five input arrays the tensor maps v, c, wx, wy,
-// wz describe (in kernel parameters for a single grid; in device memory for
-// the batch table).  Writes vn / cn.  Returns true when a bounded wait ran out
-// (after its own loads in flight have landed).
-__device__ __forceinline__ bool tb2_tile(const CUtensorMap *map_v, const CUtensorMap *map_c,
-                                         const CUtensorMap *map_wx, const CUtensorMap *map_wy,
-                                         const CUtensorMap *map_wz, float *__restrict__ vn,
+// [kb, ke), of a field whose five input arrays the maps describe.  Writes vn
+// / cn.  When a bounded wait runs out it sets *err and returns once its own
+// loads in flight have landed.
+template <class M>
+__device__ __forceinline__ void tb2_tile(const M &maps, float *__restrict__ vn,
                                          uint16_t *__restrict__ cn, int x0, int y0, int nx,
                                          int ny, int nz, int P, size_t S, int kb, int ke,
-                                         unsigned wait_limit) {
+                                         int *__restrict__ err, unsigned wait_limit) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
   const int tid = threadIdx.x;
@@ -124,11 +143,11 @@ __device__ __forceinline__ bool tb2_tile(const CUtensorMap *map_v, const CUtenso
     unsigned long long *b = &sm.bar[s];
     tma::fence_proxy_async();
     mbar_expect(b, kSlotBytes);
-    tma_load3(sl.v, map_v, X0, Y0, p, b);
-    tma_load3(sl.wx, map_wx, X0, Y0, p, b);
-    tma_load3(sl.wy, map_wy, X0, Y0, p, b);
-    tma_load3(sl.wz, map_wz, X0, Y0, p, b);
-    tma_load3(sl.c, map_c, X0c, Y0, p, b);
+    tma_load3(sl.v, maps.v(), X0, Y0, p, b);
+    tma_load3(sl.wx, maps.wx(), X0, Y0, p, b);
+    tma_load3(sl.wy, maps.wy(), X0, Y0, p, b);
+    tma_load3(sl.wz, maps.wz(), X0, Y0, p, b);
+    tma_load3(sl.c, maps.c(), X0c, Y0, p, b);
   };
   auto wait_plane = [&](int p) {
     if (!waiter || p < pmin || p > pmax || failed) return;
@@ -290,13 +309,14 @@ __device__ __forceinline__ bool tb2_tile(const CUtensorMap *map_v, const CUtenso
     ib = ic;
     ic = t3;
   }
-  if (failed && waiter) {
+  if (failed) {
+    if (tid == 0) atomicExch(err, 1);
     // Let the block's own loads in flight land before its shared memory goes
     // (each wait bounded).
-    for (int s = 0; s < R; ++s)
-      if (pending & (1u << s)) mbar_wait(&sm.bar[s], (phase >> s) & 1u);
+    if (waiter)
+      for (int s = 0; s < R; ++s)
+        if (pending & (1u << s)) mbar_wait(&sm.bar[s], (phase >> s) & 1u);
   }
-  return failed;
 }
 
 __global__ void __launch_bounds__(NT, 2)
@@ -306,10 +326,8 @@ __global__ void __launch_bounds__(NT, 2)
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
   if (kb >= ke) return;
-  if (tb2_tile(&in.v, &in.c, &in.wx, &in.wy, &in.wz, vn, cn, 1 + OX * blockIdx.x,
-               1 + OY * blockIdx.y, nx, ny, nz, P, S, kb, ke, wait_limit) &&
-      threadIdx.x == 0)
-    atomicExch(err, 1);
+  tb2_tile(ParamMaps{in}, vn, cn, 1 + OX * blockIdx.x, 1 + OY * blockIdx.y, nx, ny, nz, P, S, kb,
+           ke, err, wait_limit);
 }
 
 // The batch table's two-step FP32C tiles: one block per tile, hardware
@@ -328,11 +346,8 @@ __global__ void __launch_bounds__(NT, 2)
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tm + threadIdx.x)
                  : "memory");
   __syncthreads();
-  if (tb2_tile(&tm[src], &tm[2 + src], &tm[4], &tm[5], &tm[6], (float *)g.f[dst], g.cr[dst],
-               1 + OX * tl.tx, 1 + OY * tl.ty, g.nx, g.ny, g.nz, g.P, g.S, tl.k0, tl.k1,
-               kWaitLimit) &&
-      threadIdx.x == 0)
-    atomicExch(g.err, 1);
+  tb2_tile(TableMaps{tm, src}, (float *)g.f[dst], g.cr[dst], 1 + OX * tl.tx, 1 + OY * tl.ty, g.nx,
+           g.ny, g.nz, g.P, g.S, tl.k0, tl.k1, g.err, kWaitLimit);
 }
 
 bool encode(CUtensorMap *m, const void *base, bool bf16, const heat_geom &g) {
