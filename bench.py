@@ -301,6 +301,21 @@ def our_arm(a):
 
     # ---- end to end through the ABI from pinned host memory, timed per call
     # (right after the device-timed leg, before any other context exists)
+    # The host link's own speed just before the leg (a torch copy of u0 each
+    # way between the pinned buffers and the device): the copies inside
+    # heat_init / heat_get_field cannot beat it, and on a shared host it varies
+    # from run to run.
+    dbuf = torch.empty(pu.shape, dtype=torch.float64, device="cuda")
+    link = {}
+    for name, src_t, dst_t in (("h2d_gbs", pu, dbuf), ("d2h_gbs", dbuf, pout)):
+        dst_t.copy_(src_t, non_blocking=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            dst_t.copy_(src_t, non_blocking=True)
+        torch.cuda.synchronize()
+        link[name] = round(3 * pu.numel() * 8 / (time.perf_counter() - t0) / 1e9, 1)
+    del dbuf
     e2e_steps = max(1, min(a.steps, 3))
     phase_names = ("heat_init", "heat_step", "heat_get_field", "heat_destroy")
     phases = dict.fromkeys(phase_names, 0.0)
@@ -404,6 +419,7 @@ def our_arm(a):
                     "d2h_bytes_per_step": int(pout.numel() * 8),
                     "ms_per_step": round(e2e_s * 1e3, 3),
                     "phases_ms": {k: round(v * 1e3 / e2e_steps, 3) for k, v in phases.items()},
+                    "host_link": link,
                     "clocks": e2e_clk.summary()},
             "fp32c": {"value": round(fp32c_value, 3), "unit": UNIT,
                       "vs_fp64": round(fp32c_value / (value / world), 3),

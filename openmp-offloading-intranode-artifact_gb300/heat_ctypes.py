@@ -125,6 +125,7 @@ SIGNATURES = {
     "heat_diag_field_diff": (C.c_int, [C.c_void_p, C.c_void_p, _dp, _dp]),
     "heat_diag_wait_timeout": (C.c_int, [C.c_uint, C.POINTER(C.c_int)]),
     "heat_diag_fp32c_timeout": (C.c_int, [C.c_void_p]),
+    "heat_diag_fp64_timeout": (C.c_int, [C.c_void_p]),
 }
 
 

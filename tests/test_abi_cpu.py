@@ -125,3 +125,39 @@ def test_config2_kappa_is_smoothed(heat):
     # smoothing shrinks the spread of log kappa well below sigma = 1
     assert np.log(kappa).std() < 0.5
     assert np.all(np.isfinite(kappa))
+
+
+def test_tune_choice_rejects_bad_arguments_without_a_device(heat):
+    lib = heat.lib()
+    e = heat.HeatTuneEntry()
+    assert lib.heat_tune_choice(heat.HEAT_FP64, 0, 64, None) == heat.HEAT_EINVAL
+    assert lib.heat_tune_choice(heat.HEAT_FP64, 0, 2, C.byref(e)) == heat.HEAT_EINVAL
+    assert lib.heat_tune_choice(7, 0, 64, C.byref(e)) == heat.HEAT_EINVAL
+
+
+def test_tune_choice_reads_a_written_cache(heat, tmp_path, monkeypatch):
+    """The cache is read again when its path changes; entries written before
+    rows / minb / depth existed read with the defaults."""
+    cache = tmp_path / "t.json"
+    cache.write_text('{"device": "x", "entries": [\n'
+                     ' {"form": 3, "nz_max": 128, "kchunk": 24, "rows": 2, "minb": 3, "depth": 2, "glups": 1.0},\n'
+                     ' {"form": 0, "nz_max": 128, "kchunk": 40, "glups": 1.0}\n]}\n')
+    monkeypatch.setenv("HEAT_TUNE_CACHE", str(cache))
+    assert heat.tune_choice(heat.HEAT_FP32C, 0, 100) == {"kchunk": 24, "rows": 2, "blocks_per_sm": 3,
+                                                        "depth": 2}
+    assert heat.tune_choice(heat.HEAT_FP64, 0, 100) == {"kchunk": 40, "rows": 1, "blocks_per_sm": 3,
+                                                       "depth": 1}
+    assert heat.tune_lookup(heat.HEAT_FP64, 0, 100) == 40
+    # another class of the same cache, not tuned: the defaults
+    assert heat.tune_choice(heat.HEAT_FP32C, 0, 300) == {"kchunk": 32, "rows": 1, "blocks_per_sm": 4,
+                                                        "depth": 1}
+
+
+def test_bench_reads_the_traffic_record():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    t, src = bench.profile_traffic(510 ** 3)
+    assert src and 30 < src["bytes_per_update"] < 60
+    assert t == pytest.approx(src["bytes_per_update"] * 510 ** 3, rel=1e-3)

@@ -7,6 +7,7 @@
     attempts, gives up, flags its context and returns; heat_sync, heat_norm,
     heat_get_field and heat_batch_run each report HEAT_ETIMEOUT (once), the
     context's field is untouched, and solves after it still match the oracle;
+  - the same for the default FP64 form's TMA-staged launch;
   - a context larger than the device returns HEAT_ENOMEM from its first device
     allocation (before any host data is read) and leaves nothing behind.
 """
@@ -111,3 +112,29 @@ def test_product_kernel_timeout_needs_the_two_step_form(H):
         assert H.lib().heat_diag_fp32c_timeout(s._ctx) == H.HEAT_ESTATE
     with H.Solver(kappa, u0, h, dt, precision=H.HEAT_FP32C, flags=H.HEAT_NO_TEMPORAL) as s:
         assert H.lib().heat_diag_fp32c_timeout(s._ctx) == H.HEAT_ESTATE
+
+
+def test_default_fp64_kernel_timeout(H, oracle):
+    """The TMA-staged default FP64 launch's own failure path: both warpgroups
+    give up at their first wait, nothing is written, the status surfaces once,
+    and the context's next steps equal a fresh context's."""
+    kappa, u0, h, dt = H.inputs_config(1, 4, 70, 45, 38)
+    with H.Solver(kappa, u0, h, dt) as s:
+        s.step(3)
+        before = s.field()
+        lib = H.lib()
+        assert lib.heat_diag_fp64_timeout(s._ctx) == H.HEAT_OK
+        out = np.empty_like(before)
+        assert lib.heat_get_field(s._ctx, out.ctypes.data) == H.HEAT_ETIMEOUT
+        assert bits_equal(out, before)
+        assert lib.heat_sync(s._ctx) == H.HEAT_OK
+        assert lib.heat_diag_fp64_timeout(s._ctx) == H.HEAT_OK
+        assert lib.heat_sync(s._ctx) == H.HEAT_ETIMEOUT
+        s.step(4)
+        got = s.field()
+    with H.Solver(kappa, u0, h, dt) as ref:
+        ref.step(7)
+        assert bits_equal(got, ref.field())
+    with H.Solver(kappa, u0, h, dt, flags=H.HEAT_BITEXACT) as s:
+        assert H.lib().heat_diag_fp64_timeout(s._ctx) == H.HEAT_ESTATE
+    assert small_solve_matches_oracle(H, oracle)
