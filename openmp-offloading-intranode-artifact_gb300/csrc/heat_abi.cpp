@@ -289,6 +289,16 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
       if (v >= 0 && v <= 8) c->hw_rows = v;
     }
     if (c->hw_rows == 8) use_int = false;
+    // Both weight sets (the hybrid's two kinds of rows) come from one fused
+    // pass; HEAT_SETUP_SPLIT=1 runs the two separate kernels instead (same
+    // values; for comparison).
+    const char *sp = std::getenv("HEAT_SETUP_SPLIT");
+    const bool fused = use_int && c->hw_rows > 0 && !(sp && sp[0] == '1') &&
+                       g.ny <= 65535;  // one grid row of blocks per grid row j
+    if (fused) {
+      TRY(dalloc(&c->c0, g.elems, c->stream));
+      for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems, c->stream));
+    }
     if (use_int) {
       // Integer-pipe form: per-point fixed-point factor*kappa.  Falls back to
       // the FP64-pipe kernel when the fixed-point range check fails.
@@ -296,7 +306,10 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
       int bad = 0;
       int *d_bad = reinterpret_cast<int *>(c->partials);
       cudaError_t e = cudaMemsetAsync(d_bad, 0, sizeof(int), c->stream);
-      if (e == cudaSuccess) e = heat::launch_kq_setup(c->kq, d_bad, kap, g, c->factor, c->stream);
+      if (e == cudaSuccess)
+        e = fused ? heat::launch_weights_setup(c->kq, c->c0, c->cf, d_bad, kap, g, c->factor,
+                                               c->stream)
+                  : heat::launch_kq_setup(c->kq, d_bad, kap, g, c->factor, c->stream);
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(&bad, d_bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
       if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
@@ -308,7 +321,7 @@ int init_fp64(heat_ctx *c, const heat_desc *d) {
         use_int = false;
       }
     }
-    if (!use_int || c->hw_rows > 0) {
+    if (!fused && (!use_int || c->hw_rows > 0)) {
       TRY(dalloc(&c->c0, g.elems, c->stream));
       for (int a = 0; a < 3; ++a) TRY(dalloc(&c->cf[a], g.elems, c->stream));
       cudaError_t e = heat::launch_fast_coeffs(c->c0, c->cf, kap, g, c->factor, c->stream);

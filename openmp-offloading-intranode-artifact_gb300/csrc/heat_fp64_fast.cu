@@ -31,16 +31,13 @@ __global__ void k_fast_coeffs(double *__restrict__ c0, double *__restrict__ cx,
     const size_t c = (size_t)k * S + (size_t)j * P + i;
     bool in = i < nx;
     double kc = in ? kap[c] : 0.0;
-    cx[c] = (i + 1 < nx) ? factor * (kc + kap[c + 1]) : 0.0;
-    cy[c] = (in && j + 1 < ny) ? factor * (kc + kap[c + P]) : 0.0;
-    cz[c] = (in && k + 1 < nz) ? factor * (kc + kap[c + S]) : 0.0;
+    cx[c] = (i + 1 < nx) ? fw(factor, kc, kap[c + 1]) : 0.0;
+    cy[c] = (in && j + 1 < ny) ? fw(factor, kc, kap[c + P]) : 0.0;
+    cz[c] = (in && k + 1 < nz) ? fw(factor, kc, kap[c + S]) : 0.0;
     double w = 0.0;
-    if (in && i > 0 && j > 0 && k > 0 && i < nx - 1 && j < ny - 1 && k < nz - 1) {
-      double e = factor * (kc + kap[c + 1]), ww = factor * (kap[c - 1] + kc);
-      double n = factor * (kc + kap[c + P]), s = factor * (kap[c - P] + kc);
-      double up = factor * (kc + kap[c + S]), dn = factor * (kap[c - S] + kc);
-      w = 1.0 - (((((e + ww) + n) + s) + up) + dn);
-    }
+    if (in && i > 0 && j > 0 && k > 0 && i < nx - 1 && j < ny - 1 && k < nz - 1)
+      w = centre(fw(factor, kc, kap[c + 1]), fw(factor, kap[c - 1], kc), fw(factor, kc, kap[c + P]),
+                 fw(factor, kap[c - P], kc), fw(factor, kc, kap[c + S]), fw(factor, kap[c - S], kc));
     c0[c] = w;
   }
 }

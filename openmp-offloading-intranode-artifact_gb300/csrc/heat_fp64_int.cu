@@ -121,7 +121,86 @@ __global__ void k_kq_setup(u64 *__restrict__ K, int *__restrict__ bad,
 }
 
 
+// k_kq_setup and k_fast_coeffs (heat_fp64_fast.cu) in one pass, the same
+// values bit for bit (both form the weights with fw / centre, every operation
+// rounded on its own, so no contraction choice of the compiler can differ): each
+// thread walks one (i, j) column over a chunk of planes, keeping kappa and the
+// z-face weight of the plane below in registers, so a point forms its three
+// stored face weights cx, cy, cz, re-forms only the two lower in-plane ones
+// (cx[c-1], cy[c-P]; same operands, same rounding) for its centre weight
+//   c0 = 1 - (((((cx[c] + cx[c-1]) + cy[c]) + cy[c-P]) + cz[c]) + cz[c-S]),
+// and takes the fixed-point check from the same sum: a centre weight below
+// 2^-40 (k_kq_setup's bound on factor * sum of the six kappa sums; the two sums
+// differ by a few ulps) marks the problem as outside the fixed-point range.
+// About 22 FP64 operations per point against 42 for the two kernels.
+__global__ void __launch_bounds__(256)
+    k_weights_setup(u64 *__restrict__ K, double *__restrict__ c0, double *__restrict__ cx,
+                    double *__restrict__ cy, double *__restrict__ cz, int *__restrict__ bad,
+                    const double *__restrict__ kap, int nx, int ny, int nz, int P, size_t S,
+                    double factor, int kchunk) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  const int k0 = blockIdx.z * kchunk;
+  const int k1 = min(k0 + kchunk, nz);
+  if (i >= P || k0 >= k1) return;
+  size_t c = (size_t)k0 * S + (size_t)j * P + i;
+  if (i >= nx) {  // padding column
+    for (int k = k0; k < k1; ++k, c += S) {
+      K[c] = 0;
+      c0[c] = cx[c] = cy[c] = cz[c] = 0.0;
+    }
+    return;
+  }
+  bool ok_all = true;
+  double kc = kap[c];
+  double zd = (k0 > 0) ? fw(factor, kap[c - S], kc) : 0.0;  // cz of the plane below
+  for (int k = k0; k < k1; ++k, c += S) {
+    const double ku = (k + 1 < nz) ? kap[c + S] : 0.0;
+    // fixed-point weight, as k_kq_setup
+    const double p = factor * kc;
+    const double q = fma(factor, kc, -p);
+    bool ok = isfinite(kc) && kc >= 0.0 && isfinite(p) && p < 0.25;
+    u64 v = 0;
+    if (ok) {
+      v = __double2ull_rn(p * 0x1p64);
+      v = (u64)((i64)v + __double2ll_rn(q * 0x1p64));
+    }
+    K[c] = v;
+    // face weights, as k_fast_coeffs
+    const double wx = (i + 1 < nx) ? fw(factor, kc, kap[c + 1]) : 0.0;
+    const double wy = (j + 1 < ny) ? fw(factor, kc, kap[c + P]) : 0.0;
+    const double wz = (k + 1 < nz) ? fw(factor, kc, ku) : 0.0;
+    cx[c] = wx;
+    cy[c] = wy;
+    cz[c] = wz;
+    double w = 0.0;
+    if (i > 0 && j > 0 && k > 0 && i < nx - 1 && j < ny - 1 && k < nz - 1) {
+      w = centre(wx, fw(factor, kap[c - 1], kc), wy, fw(factor, kap[c - P], kc), wz, zd);
+      if (ok && !(w >= 0x1p-40)) ok = false;
+    }
+    c0[c] = w;
+    ok_all &= ok;
+    zd = wz;
+    kc = ku;
+  }
+  if (!ok_all) atomicOr(bad, 1);
+}
+
 }  // namespace
+
+cudaError_t launch_weights_setup(unsigned long long *K, double *c0, double *const cf[3], int *bad,
+                                 const double *kappa, const heat_geom &g, double factor,
+                                 cudaStream_t st) {
+  // z-chunks so that the columns times chunks reach ~2048 threads per SM
+  const long cols = (long)g.pitch * g.ny;
+  const long want = 152L * 2048;
+  const int chunks = (int)std::max(1L, std::min<long>(g.nz, (want + cols - 1) / cols));
+  const int kc = (g.nz + chunks - 1) / chunks;
+  dim3 gr((g.pitch + 255) / 256, g.ny, (g.nz + kc - 1) / kc);
+  k_weights_setup<<<gr, 256, 0, st>>>(K, c0, cf[0], cf[1], cf[2], bad, kappa, g.nx, g.ny, g.nz,
+                                      g.pitch, g.plane, factor, kc);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_kq_setup(unsigned long long *K, int *bad, const double *kappa,
                             const heat_geom &g, double factor, cudaStream_t st) {

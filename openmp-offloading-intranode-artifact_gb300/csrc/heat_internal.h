@@ -59,6 +59,20 @@ struct heat_ctx {
 // ---- kernel launchers (each returns cudaError_t of the launch) ----------
 namespace heat {
 
+#ifdef __CUDACC__
+// Face weight factor * (ka + kb) and centre weight
+// 1 - (((((e + w) + n) + s) + u) + d) of the default FP64 form, every operation
+// rounded on its own (no fused multiply-add), so every kernel that forms them
+// gets the same bits.
+__device__ __forceinline__ double fw(double factor, double ka, double kb) {
+  return __dmul_rn(factor, __dadd_rn(ka, kb));
+}
+__device__ __forceinline__ double centre(double e, double w, double n, double s, double u,
+                                         double d) {
+  return __dsub_rn(1.0, __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(e, w), n), s), u), d));
+}
+#endif
+
 constexpr int kNormBlocks = 152 * 4;   // partial-sum blocks of the norm pass
 
 // Bound of every device-side mbarrier wait in the TMA kernels (try_wait
@@ -101,6 +115,10 @@ cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
                         cudaStream_t st);
 
 // heat_fp64_int.cu
+// K and c0, cx, cy, cz in one pass (the two kernels below, fused; same values).
+cudaError_t launch_weights_setup(unsigned long long *K, double *c0, double *const cf[3], int *bad,
+                                 const double *kappa, const heat_geom &g, double factor,
+                                 cudaStream_t st);
 cudaError_t launch_kq_setup(unsigned long long *K, int *bad, const double *kappa,
                             const heat_geom &g, double factor, cudaStream_t st);
 // hw_rows of the 8 warps in each block take the FP64 pipe, the rest the

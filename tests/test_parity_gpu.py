@@ -248,3 +248,20 @@ def test_heat_update_dropin_uneven_no_rhs(H, oracle, cuda_device):
         a, b = b, a
     torch.cuda.synchronize()
     assert bits_equal(a.cpu().numpy(), oracle.steps(u0, kappa, h, dt, 6))
+
+
+@pytest.mark.parametrize("cfg,shape", [(1, (96, 80, 72)), (0, (37, 29, 130))])
+def test_fused_weight_setup_equals_the_separate_kernels(H, monkeypatch, cfg, shape):
+    """The default form's set-up forms the fixed-point and the FP64 weights in
+    one pass; the two separate set-up kernels give the same weights, so the
+    same fields bit for bit."""
+    nx, ny, nz = shape
+    kappa, u0, h, dt = H.inputs_config(cfg, 9, nx, ny, nz)
+    with H.Solver(kappa, u0, h, dt) as s:
+        s.step(11)
+        fused = s.field()
+    monkeypatch.setenv("HEAT_SETUP_SPLIT", "1")
+    with H.Solver(kappa, u0, h, dt) as s:
+        s.step(11)
+        split = s.field()
+    assert bits_equal(fused, split)
