@@ -150,16 +150,21 @@ def test_config1_full_size_short(H, oracle):
     assert m["max_rel"] <= FAST_MAX_REL, m
 
 
-def test_config1_full_size_1000_steps_properties(H):
-    """Config 1 exactly (512^3, 1000 steps): the default form against the
-    bit-exact form on the GPU (the bit-exact form equals the oracle above),
-    and size-independent properties: zero boundary kept, maximum principle
-    (no new extrema without a source), heat leaves through the boundary."""
+def test_config1_full_size_1000_steps(H, oracle):
+    """Config 1 exactly (512^3, 1000 steps) against the oracle (about 30 s of
+    the host's cores): the bit-exact form bit for bit, the default form to
+    <= 1e-12 max-rel; and size-independent properties: zero boundary kept,
+    maximum principle (no new extrema without a source), heat leaves through
+    the boundary."""
     kappa, u0, h, dt = H.inputs_config(1, 1, 512, 512, 512)
+    u_or = oracle.steps(u0, kappa, h, dt, 1000)
     u_ex, _, (l2e, cse) = solve(H, kappa, u0, h, dt, steps=1000, flags=1)
+    assert bits_equal(u_ex, u_or)
+    del u_ex
     u_fa, _, (l2f, csf) = solve(H, kappa, u0, h, dt, steps=1000, flags=0)
-    m = metrics(u_ex, u_fa)
+    m = metrics(u_or, u_fa)
     assert m["max_rel"] <= FAST_MAX_REL and m["rel_l2"] <= FAST_REL_L2, m
+    del u_or
     b = np.ones(u_fa.shape, dtype=bool)
     b[1:-1, 1:-1, 1:-1] = False
     assert np.all(u_fa[b] == 0.0)
