@@ -145,12 +145,14 @@ const char *heat_strerror(int status);
  * holds contexts of any size and form (HEAT_FP64 default or HEAT_BITEXACT,
  * HEAT_FP32C; not HEAT_NAIVE) on one device.  heat_batch_run advances every
  * context that still has scheduled steps by one step per launch of one kernel
- * per kind present (form x source term), each walking a tile table over all
- * grids of its kind; runs of 16 steps are captured once as a CUDA graph and
- * replayed.  Per-context results are
- * identical to heat_step on the context alone.  While a context is in a
- * batch, step it through the batch (stepping it directly is detected and the
- * batch rebuilds its table).                                                   */
+ * per kind present (form x source term x the tuned blocks-per-SM variant),
+ * each walking a tile table over all grids of its kind (FP32C grids whose
+ * size class the tuner gave two steps per launch advance in pairs of steps);
+ * grids of at least 2 M interior points step with their single-grid kernels
+ * beside the table; runs of 16 steps are captured once as a CUDA graph and
+ * replayed.  Per-context results are identical to heat_step on the context
+ * alone.  While a context is in a batch, step it through the batch (stepping
+ * it directly is detected and the batch rebuilds its table).                  */
 typedef struct heat_batch heat_batch;
 #define HEAT_BATCH_NO_GRAPHS     0x1u  /* plain launches only                  */
 #define HEAT_BATCH_PERSISTENT    0x2u  /* resident blocks stride the tile table */

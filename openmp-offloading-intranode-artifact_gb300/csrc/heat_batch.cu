@@ -1,12 +1,15 @@
-// Batched persistent kernel: one launch advances every grid of a batch by one
-// time step.  The host builds a tile table -- (grid, tile x, tile y, z range)
-// entries over all active grids -- and a fixed set of resident blocks strides
-// through it (tile t goes to block t mod gridDim.x).  Each tile is a (32 x 8)
-// set of (i, j) columns walking its z range with the same column walks the
-// single-grid kernels use (heat_walk.cuh), so a grid's results are identical
-// alone and in a batch.  Grids of different precision forms and sizes share a
-// launch; no block ever waits on another, so the kernel needs no grid-wide
-// synchronisation and cannot deadlock.
+// Batched table kernels: one launch per kind advances every grid of that kind
+// in a batch by one time step.  The host builds a tile table -- (grid, tile x,
+// tile y, z range, rows per thread) entries over all active grids -- and the
+// blocks stride through it (tile t goes to block t mod gridDim.x; by default
+// one block per tile).  Each tile is a 32 x (8 * rows) set of (i, j) columns
+// walking its z range with the same column walks the single-grid kernels use
+// (heat_walk.cuh), so a grid's results are identical alone and in a batch,
+// whatever the tile shape and blocks-per-SM variant the autotuner picked.
+// Grids of different sizes share a launch; no block ever waits on another, so
+// the kernels need no grid-wide synchronisation and cannot deadlock.  (FP32C
+// grids the tuner gave two steps per launch run k_batch_fp32c_tb2 in
+// heat_fp32c_tma.cu instead.)
 
 #include "heat_batch_internal.h"
 #include "heat_walk.cuh"

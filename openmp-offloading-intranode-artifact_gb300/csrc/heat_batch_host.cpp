@@ -7,8 +7,11 @@
 // instead.  On configuration 3 (64 uneven grids, half FP64, half FP32C) the
 // hardware-scheduled shape measured 92 GLUP/s against 86 for the persistent
 // one, whose blocks serialise each tile's start-up loads.  Kinds (form x
-// source term) present together run on their own streams, forked from and
-// joined to the batch stream, unless HEAT_BATCH_SERIAL_FORMS.
+// source term x blocks-per-SM variant) present together run on their own
+// streams (created on first use), forked from and joined to the batch stream,
+// unless HEAT_BATCH_SERIAL_FORMS.  Each grid's z-chunk, rows per thread,
+// variant and (FP32C) temporal depth come from the autotuner's cache for its
+// depth class (heat_tune.cpp).
 //
 // Grids large enough to fill the GPU alone (HEAT_BATCH_SOLO_POINTS interior
 // points, default 2,000,000) are stepped with their single-grid kernels
@@ -23,8 +26,11 @@
 // launch gets the parity of the steps taken since.  A captured graph records
 // every grid's current buffer, and is replayed only while they match (a run
 // of an even number of steps returns table grids to the same buffers, and
-// two-step launches swap once per two steps).  The table is rebuilt (and the
-// graph re-captured) when the set of active contexts changes.
+// two-step launches swap once per two steps).  Table grids with two steps per
+// launch ("pairs") swap like solo grids: n steps are n / 2 two-step table
+// launches (flips counted from pair_flips) and, for an odd n, one single step
+// with the grid's own kernel.  The table is rebuilt (and the graph
+// re-captured) when the set of active contexts changes.
 
 #include <algorithm>
 #include <cstdio>
