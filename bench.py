@@ -279,32 +279,16 @@ def our_arm(a):
     stream = torch.cuda.Stream()
     fp64_peak = H.fp64_rate()
 
-    # ---- device-resident value
-    s = H.Solver(kappa, u0, h, dt, stream=stream.cuda_stream)
-    for _ in range(a.warmup):
-        s.step(ts)
-    s.sync()
-    _, l0 = s.stats()
-    barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev) as clk:
-        ev0.record(stream)
-        for _ in range(a.steps):
-            s.step(ts)
-        ev1.record(stream)
-        ev1.synchronize()
-    barrier()
-    _, l1 = s.stats()
-    ms = ev0.elapsed_time(ev1)
-    l2n, csum = s.norm()
-    s.close()
-
-    # ---- end to end through the ABI from pinned host memory, timed per call
-    # (right after the device-timed leg, before any other context exists)
-    # The host link's own speed just before the leg (a torch copy of u0 each
-    # way between the pinned buffers and the device): the copies inside
-    # heat_init / heat_get_field cannot beat it, and on a shared host it varies
-    # from run to run.
+    # ---- end to end through the ABI from pinned host memory, timed per call.
+    # It runs before the long device-timed leg: after seconds of compute
+    # without transfers the host link can be slow for a while (on one box a
+    # torch copy of 1 GiB took 49 ms H2D and 187 ms D2H right after a 20-solve
+    # leg, 5 ms each once copies flowed), and this leg moves data around every
+    # solve.  Whether the link is in that state also depends on what ran on
+    # the box before; `host_link` records it: the link's warm speed just before
+    # the leg (a torch copy of u0 each way between the pinned buffers and the
+    # device, repeated), and one plain torch copy each way straight after a
+    # solve, as heat_get_field and the next heat_init meet the link.
     dbuf = torch.empty(pu.shape, dtype=torch.float64, device="cuda")
     link = {}
     for name, src_t, dst_t in (("h2d_gbs", pu, dbuf), ("d2h_gbs", dbuf, pout)):
@@ -335,9 +319,39 @@ def our_arm(a):
             if i > 0:
                 for nm, a0, a1 in zip(phase_names, t, t[1:]):
                     phases[nm] += a1 - a0
+    dbuf = torch.empty(pu.shape, dtype=torch.float64, device="cuda")
+    with H.Solver(pk.numpy(), pu.numpy(), h, dt, stream=stream.cuda_stream) as e:
+        for name, src_t, dst_t in (("h2d_after_solve_ms", pu, dbuf), ("d2h_after_solve_ms", dbuf, pout)):
+            e.step(ts)
+            e.sync()
+            t0 = time.perf_counter()
+            dst_t.copy_(src_t, non_blocking=True)
+            torch.cuda.synchronize()
+            link[name] = round((time.perf_counter() - t0) * 1e3, 2)
+    del dbuf
     e2e_t = sum(phases.values())
     e2e_s = max_over_ranks(e2e_t / e2e_steps, dist, "cuda")
     e2e_value = replica_value(updates(n, ts), world, e2e_s)
+
+    # ---- device-resident value
+    s = H.Solver(kappa, u0, h, dt, stream=stream.cuda_stream)
+    for _ in range(a.warmup):
+        s.step(ts)
+    s.sync()
+    _, l0 = s.stats()
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        ev0.record(stream)
+        for _ in range(a.steps):
+            s.step(ts)
+        ev1.record(stream)
+        ev1.synchronize()
+    barrier()
+    _, l1 = s.stats()
+    ms = ev0.elapsed_time(ev1)
+    l2n, csum = s.norm()
+    s.close()
 
     # ---- FP32-compensated form on the same inputs (precision pattern):
     # rate by CUDA events, error against the default FP64 form at 100 and ts
