@@ -113,10 +113,10 @@ int heat_norm(heat_ctx *c, double *l2, double *checksum);
  * of cudaFree/cudaMalloc.  Its scratch is a static device array sized for
  * nz <= HEAT_NORM_NOALLOC_MAX_NZ planes (256 KiB, held by every GPU that loads
  * the library); larger nz returns HEAT_EINVAL.  The first call on a device
- * looks the array's address up (do it before any stream capture).  All calls
- * on a device share the array: calls that overlap on the GPU race, so issue
- * them from one stream.  Runs on stream (cudaStream_t, NULL = legacy default)
- * and synchronises it.  Summation order differs from heat_norm's, so results
+ * looks the array's address up.  All calls on a device share the array:
+ * calls that overlap on the GPU race, so issue them from one stream.  Runs on
+ * stream (cudaStream_t, NULL = legacy default) and synchronises it, so it
+ * cannot be captured into a CUDA graph.  Summation order differs from heat_norm's, so results
  * agree with it to rounding (<= 1e-13 relative), not bit for bit.          */
 #define HEAT_NORM_NOALLOC_MAX_NZ 16384
 int heat_norm_noalloc(const double *u, int nz, int ny, int nx, double *l2,
