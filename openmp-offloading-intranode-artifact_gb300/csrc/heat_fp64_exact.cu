@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(TX *TY)
 template <bool RHS, bool RAW>
 void launch_rows(double *u_new, const double *u_old, const double *rhs, const double *kappa,
                  double *const ks[3], const heat_geom &g, double factor, cudaStream_t st) {
-  const int kc = plane_chunk(g, SX, TY * RY);
+  static const long resident = resident_blocks((const void *)k_exact_rows<RHS, RAW>, TX * TY, 0);
+  const int kc = wave_chunk(g, SX, TY * RY, resident);
   dim3 gr((g.nx - 2 + SX - 1) / SX, (g.ny - 2 + TY * RY - 1) / (TY * RY),
           (g.nz - 2 + kc - 1) / kc);
   k_exact_rows<RHS, RAW><<<gr, dim3(TX, TY), 0, st>>>(

@@ -240,7 +240,9 @@ template <bool RHS, int MINB = 4, int REGS = kWsRegs>
 void launch_ws(double *u_new, const double *u_old, const double *rhs,
                const unsigned long long *K, const double *c0, double *const cf[3],
                const heat_geom &g, cudaStream_t st) {
-  const int kc = plane_chunk(g, TX, TY);
+  static const long resident =
+      resident_blocks((const void *)k_fast_ws<RHS, MINB, REGS>, TX * TY, 0);
+  const int kc = wave_chunk(g, TX, TY, resident);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   k_fast_ws<RHS, MINB, REGS><<<gr, dim3(TX, TY), 0, st>>>(u_new, u_old, rhs, K, c0, cf[0], cf[1],
                                                           cf[2], g.nx, g.ny, g.nz, g.pitch,

@@ -392,7 +392,8 @@ cudaError_t launch_fast_tma(double *u_new, const double *u_old, const unsigned l
       !encode_f64(&m.cz, cf[2], g, 4) || !encode_f64(&m.cy, cf[1], g, 5))
     return cudaErrorInvalidValue;
   if (wait_limit > tma::kWaitLimit) wait_limit = tma::kWaitLimit;
-  const int kc = plane_chunk(g, TX, TY);
+  static const long resident = resident_blocks((const void *)k_fast_tma<>, TX * TY, tma_smem());
+  const int kc = wave_chunk(g, TX, TY, resident);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   k_fast_tma<><<<gr, dim3(TX, TY), tma_smem(), st>>>(m, u_new, g.nx, g.ny, g.nz, g.pitch,
                                                      g.plane, kc, err, wait_limit);
