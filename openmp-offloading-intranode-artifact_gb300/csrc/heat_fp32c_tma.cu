@@ -401,9 +401,9 @@ cudaError_t launch_fp32c_tb2(float *v_new, uint16_t *c_new, const float *v, cons
   // Each chunk recomputes step t+1 on its halo planes, so chunks are deeper
   // than the single-step launches': 96 planes at least (512^3: 330 GLUP/s,
   // against 324 / 320 / 309 for 64 / 48 / 32 and 311 for 128, where 3 chunks
-  // leave 5.05 waves).
+  // leave 5.05 waves), 16 where a small grid needs more chunks to fill the GPU.
   static const long resident = resident_blocks((const void *)k_fp32c_tb2, NT, fp32c_tb2_smem());
-  const int kchunk = wave_chunk(g, OX, OY, resident, 24, 96);
+  const int kchunk = wave_chunk(g, OX, OY, resident, 24, 96, 16);
   dim3 grid(bx, by, (interior + kchunk - 1) / kchunk);
   k_fp32c_tb2<<<grid, NT, fp32c_tb2_smem(), st>>>(m, v_new, c_new, g.nx, g.ny, g.nz, g.pitch,
                                                   g.plane, kchunk, err, wait_limit);

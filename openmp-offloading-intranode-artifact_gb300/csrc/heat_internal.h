@@ -103,12 +103,13 @@ long resident_blocks(const void *kernel, int threads, size_t smem);
 // run `resident` at a time: enough z-chunks that the launch spans about
 // `waves` waves of resident blocks, so the last wave, which the GPU may run
 // partly empty, is a small share of it, with at least `min_planes` planes per
-// chunk (each chunk re-reads its halo planes and refills its pipeline).  At
+// chunk (each chunk re-reads its halo planes and refills its pipeline) unless
+// that would leave fewer than two waves.  At
 // 512^3 the default FP64 launch's 1,024 tiles in 3 chunks made 5.05 waves of
 // 608 blocks: 126.4 GLUP/s; 15 chunks (25 waves): 133.4.  Falls back to
 // plane_chunk when `resident` is unknown.
 inline int wave_chunk(const heat_geom &g, int tile_x, int tile_y, long resident,
-                      long waves = 24, int min_planes = 16) {
+                      long waves = 24, int min_planes = 16, int fill_planes = 8) {
   if (resident <= 0) return plane_chunk(g, tile_x, tile_y);
   const long tiles =
       (long)((g.nx - 2 + tile_x - 1) / tile_x) * ((g.ny - 2 + tile_y - 1) / tile_y);
@@ -116,6 +117,12 @@ inline int wave_chunk(const heat_geom &g, int tile_x, int tile_y, long resident,
   long chunks = (resident * waves + tiles - 1) / tiles;
   const long max_chunks = interior / min_planes > 1 ? interior / min_planes : 1;
   if (chunks > max_chunks) chunks = max_chunks;
+  // A grid too small for `waves` waves at that depth still gets two waves of
+  // blocks where chunks of `fill_planes` planes allow it, so it does not leave
+  // SMs idle.
+  long fill = (2 * resident + tiles - 1) / tiles;
+  if (fill > interior / fill_planes) fill = interior / fill_planes;
+  if (chunks < fill) chunks = fill;
   if (chunks < 1) chunks = 1;
   return (int)((interior + chunks - 1) / chunks);
 }
