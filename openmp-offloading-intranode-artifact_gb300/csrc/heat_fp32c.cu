@@ -92,7 +92,9 @@ __global__ void k_to_f32(float *__restrict__ o, const double *__restrict__ a, si
 cudaError_t launch_fp32c(float *v_new, uint16_t *c_new, const float *v, const uint16_t *cr,
                          float *const w[3], const float *rhs, const heat_geom &g,
                          cudaStream_t st) {
-  int kc = plane_chunk(g, TX, TY);
+  static const long res_rhs = resident_blocks((const void *)k_fp32c<true>, TX * TY, 0);
+  static const long res_plain = resident_blocks((const void *)k_fp32c<false>, TX * TY, 0);
+  const int kc = wave_chunk(g, TX, TY, rhs ? res_rhs : res_plain);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   dim3 b(TX, TY);
   if (rhs)

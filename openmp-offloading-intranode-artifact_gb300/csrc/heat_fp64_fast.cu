@@ -71,7 +71,9 @@ cudaError_t launch_fast_coeffs(double *c0, double *const cf[3], const double *ka
 cudaError_t launch_fast(double *u_new, const double *u_old, const double *rhs,
                         const double *c0, double *const cf[3], const heat_geom &g,
                         cudaStream_t st) {
-  int kc = plane_chunk(g, TX, TY);
+  static const long res_rhs = resident_blocks((const void *)k_fast_hw<true>, TX * TY, 0);
+  static const long res_plain = resident_blocks((const void *)k_fast_hw<false>, TX * TY, 0);
+  const int kc = wave_chunk(g, TX, TY, rhs ? res_rhs : res_plain);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
   dim3 b(TX, TY);
   if (rhs)

@@ -214,7 +214,9 @@ template <bool RHS, int TYB, int MINB>
 void launch_mix_shape(double *u_new, const double *u_old, const double *rhs,
                       const unsigned long long *K, const double *c0, double *const cf[3],
                       const heat_geom &g, int hw_rows, cudaStream_t st) {
-  const int kc = plane_chunk(g, TX, TYB, 152L * 16 * (TY / TYB));
+  static const long resident =
+      resident_blocks((const void *)k_fast_mix<RHS, TYB, MINB>, TX * TYB, 0);
+  const int kc = wave_chunk(g, TX, TYB, resident);
   dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TYB - 1) / TYB, (g.nz - 2 + kc - 1) / kc);
   k_fast_mix<RHS, TYB, MINB><<<gr, dim3(TX, TYB), 0, st>>>(
       u_new, u_old, rhs, K, c0, cf[0], cf[1], cf[2], g.nx, g.ny, g.nz, g.pitch, g.plane, kc,
