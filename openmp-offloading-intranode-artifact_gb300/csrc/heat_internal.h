@@ -96,18 +96,18 @@ inline int plane_chunk(const heat_geom &g, int tile_x, int tile_y, long want = 1
 
 // Blocks of `kernel` resident on the current GPU at once: its occupancy per
 // SM at `threads` threads and `smem` bytes of dynamic shared memory per block,
-// times the SM count; 0 when the runtime cannot say (heat_abi.cpp).
+// times the SM count; 0 when the runtime cannot say (heat_abi.cpp).  The
+// launchers look it up once per process (one GPU model per process).
 long resident_blocks(const void *kernel, int threads, size_t smem);
 
 // Planes per block for a launch of (tile_x x tile_y)-column tiles whose blocks
 // run `resident` at a time: enough z-chunks that the launch spans about
 // `waves` waves of resident blocks, so the last wave, which the GPU may run
-// partly empty, is a small share of it, with at least `min_planes` planes per
-// chunk (each chunk re-reads its halo planes and refills its pipeline) unless
-// that would leave fewer than two waves.  At
-// 512^3 the default FP64 launch's 1,024 tiles in 3 chunks made 5.05 waves of
-// 608 blocks: 126.4 GLUP/s; 15 chunks (25 waves): 133.4.  Falls back to
-// plane_chunk when `resident` is unknown.
+// partly empty, is a small share of it; at least `min_planes` planes per chunk
+// (each chunk re-reads its halo planes and refills its pipeline) unless that
+// would leave fewer than two waves.  At 512^3 the default FP64 launch's 1,024
+// tiles in 3 chunks made 5.05 waves of 608 blocks: 126.4 GLUP/s; 15 chunks
+// (25 waves): 133.4.  Falls back to plane_chunk when `resident` is unknown.
 inline int wave_chunk(const heat_geom &g, int tile_x, int tile_y, long resident,
                       long waves = 24, int min_planes = 16, int fill_planes = 8) {
   if (resident <= 0) return plane_chunk(g, tile_x, tile_y);
