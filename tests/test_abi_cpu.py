@@ -161,3 +161,18 @@ def test_bench_reads_the_traffic_record():
     t, src = bench.profile_traffic(510 ** 3)
     assert src and 30 < src["bytes_per_update"] < 60
     assert t == pytest.approx(src["bytes_per_update"] * 510 ** 3, rel=1e-3)
+
+
+def test_bench_fp64_pipe_record():
+    """The FP64-pipe rows of the default form: (j - 1) mod 8 < 4 of the interior
+    rows, 7 operations per point."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench", ROOT / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    r = bench.fp64_pipe_record(10, 1.0, 100.0)  # interior rows 1..8: rows 1-4 on the FP64 pipe
+    assert r["ops_per_launch"] == 8 * 8 * 4 * 7
+    assert r["fp64_row_share"] == 0.5
+    r = bench.fp64_pipe_record(512, 1.0, 500.0)  # 510 rows: 63 full groups of 8 and 6 more
+    assert r["ops_per_launch"] == 510 * 510 * (63 * 4 + 4) * 7
+    assert r["frac"] == pytest.approx(r["achieved_gops"] / 500.0, rel=1e-3)
