@@ -51,12 +51,12 @@ int heat_diag_wait_timeout(unsigned attempts, int *timed_out);
 int heat_diag_fp32c_timeout(struct heat_ctx *c);
 
 /* The same for the default FP64 form's TMA-staged launch (the kernel
- * heat_step uses for HEAT_FP64 contexts without a source term): one launch
- * with its wait limit at 0 attempts gives up at its first wait in both
+ * heat_step uses for HEAT_FP64 contexts, with or without a source term): one
+ * launch with its wait limit at 0 attempts gives up at its first wait in both
  * warpgroups, flags the context and returns without writing a point; the next
  * synchronising call reports HEAT_ETIMEOUT once.  HEAT_ESTATE for a context
  * that does not step with that launch (HEAT_BITEXACT, HEAT_NAIVE,
- * HEAT_HWFP64, a source term, HEAT_FP32C).                                   */
+ * HEAT_HWFP64, HEAT_FP32C).                                                  */
 int heat_diag_fp64_timeout(struct heat_ctx *c);
 
 #ifdef __cplusplus

@@ -689,11 +689,11 @@ int heat_diag_fp32c_timeout(heat_ctx *c) {
 int heat_diag_fp64_timeout(heat_ctx *c) {
   if (!c) return HEAT_EINVAL;
   // Only contexts that step with the TMA-staged default FP64 launch.
-  if (c->precision != HEAT_FP64 || !c->kq || c->rhs || c->hw_rows != 4 ||
-      !heat::fast_tma_usable(c->g))
+  if (c->precision != HEAT_FP64 || !c->kq || c->hw_rows != 4 ||
+      !heat::fast_tma_usable(c->g, c->rhs != nullptr))
     return HEAT_ESTATE;
-  cudaError_t e = heat::launch_fast_tma(c->u[c->cur ^ 1], c->u[c->cur], c->kq, c->c0, c->cf, c->g,
-                                        c->err, c->stream, 0u);
+  cudaError_t e = heat::launch_fast_tma(c->u[c->cur ^ 1], c->u[c->cur], c->kq, c->c0, c->cf,
+                                        c->rhs, c->g, c->err, c->stream, 0u);
   if (e != cudaSuccess) return cuda_fail(e, "default FP64 kernel launch");
   c->launches += 1;
   return HEAT_OK;

@@ -259,15 +259,15 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             int *err, cudaStream_t st) {
   if (hw_rows < 0) hw_rows = 0;
   if (hw_rows > 8) hw_rows = 8;
-  // Default split without a source term: the TMA-staged integer rows
-  // (heat_fp64_tma.cu), same bits as k_fast_ws; HEAT_FP64_NO_TMA=1 selects
+  // Default split: the TMA-staged launch (heat_fp64_tma.cu), same bits as
+  // k_fast_ws, with or without a source term; HEAT_FP64_NO_TMA=1 selects
   // k_fast_ws for comparison runs.
   static const bool no_tma = [] {
     const char *e = std::getenv("HEAT_FP64_NO_TMA");
     return e && e[0] == '1';
   }();
-  if (!rhs && hw_rows == 4 && err && !no_tma && fast_tma_usable(g))
-    return launch_fast_tma(u_new, u_old, K, c0, cf, g, err, st);
+  if (hw_rows == 4 && err && !no_tma && fast_tma_usable(g, rhs != nullptr))
+    return launch_fast_tma(u_new, u_old, K, c0, cf, rhs, g, err, st);
   // Default split (hw_rows = 4): k_fast_ws.  Other splits: 8-row blocks with
   // registers capped for 3 resident blocks per SM (a few spills, more warps
   // to hide the integer walk's load latency): 101 GLUP/s at 512^3 against 94

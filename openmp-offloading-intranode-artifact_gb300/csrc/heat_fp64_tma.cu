@@ -37,6 +37,8 @@
 
 #include <cuda.h>
 
+#include <cstring>
+
 #include "heat_internal.h"
 #include "heat_tma.cuh"
 #include "heat_walk.cuh"
@@ -63,32 +65,56 @@ constexpr int pad128(int rows) { return (rows * RW * 8 + 127) / 128 * 128 / 8; }
 constexpr int kIntRows = 6;
 constexpr int kIntPts = kIntRows * RW;  // 204
 constexpr int kIntPad = pad128(kIntRows);
-struct __align__(128) IntSlot {
+// With a source term each slot also holds its rows' source values (a 34 x 4
+// box at the warpgroup's own rows).
+constexpr int kRPad = pad128(4);
+template <bool RHS>
+struct __align__(128) IntSlotT {
   u64 u[kIntPad];
   u64 k[kIntPad];
 };
-constexpr unsigned kIntSlotBytes = 2u * kIntPts * 8u;  // OOB-filled boxes count in full
+template <>
+struct __align__(128) IntSlotT<true> {
+  u64 u[kIntPad];
+  u64 k[kIntPad];
+  u64 r[kRPad];
+};
+template <bool RHS>  // OOB-filled boxes count in full
+constexpr unsigned kIntSlotBytes = 2u * kIntPts * 8u + (RHS ? 4u * RW * 8u : 0u);
 
 // FP64 rows' slot: u over rows j0-1 .. j0+4, c0 / cx / cz over rows j0 .. j0+3,
 // cy over rows j0-1 .. j0+3.
 constexpr int kHwPad6 = pad128(6), kHwPad4 = pad128(4), kHwPad5 = pad128(5);
-struct __align__(128) HwSlot {
+template <bool RHS>
+struct __align__(128) HwSlotT {
   double u[kHwPad6];
   double c0[kHwPad4];
   double cx[kHwPad4];
   double cz[kHwPad4];
   double cy[kHwPad5];
 };
-constexpr unsigned kHwSlotBytes = (6u + 3u * 4u + 5u) * RW * 8u;
-static_assert(sizeof(IntSlot) % 128 == 0 && sizeof(HwSlot) % 128 == 0,
+template <>
+struct __align__(128) HwSlotT<true> {
+  double u[kHwPad6];
+  double c0[kHwPad4];
+  double cx[kHwPad4];
+  double cz[kHwPad4];
+  double cy[kHwPad5];
+  double r[kRPad];
+};
+template <bool RHS>
+constexpr unsigned kHwSlotBytes = (6u + 3u * 4u + 5u + (RHS ? 4u : 0u)) * RW * 8u;
+static_assert(sizeof(IntSlotT<false>) % 128 == 0 && sizeof(HwSlotT<false>) % 128 == 0 &&
+                  sizeof(IntSlotT<true>) % 128 == 0 && sizeof(HwSlotT<true>) % 128 == 0,
               "ring slots start on 128-byte boundaries");
 static_assert((kIntPad * 8) % 128 == 0 && (kHwPad4 * 8) % 128 == 0 && (kHwPad5 * 8) % 128 == 0 &&
                   (kHwPad6 * 8) % 128 == 0,
               "every array of a slot starts on a 128-byte boundary");
 
+template <bool RHS>
 struct SmemT {
-  HwSlot hw[NR];
-  IntSlot in[NR];
+  HwSlotT<RHS> hw[NR];
+  IntSlotT<RHS> in[NR];
   i64 m[ND][kIntPad];  // decoded significands << 9, signed
   int e[ND][kIntPad];  // decoded biased exponents (subnormals and zero: 1)
   u64 hbar[NR];
@@ -100,6 +126,7 @@ struct Maps {
   CUtensorMap k;            // box 34 x 6
   CUtensorMap c0, cx, cz;   // box 34 x 4
   CUtensorMap cy;           // box 34 x 5
+  CUtensorMap r;            // box 34 x 4 (source term; set only with one)
 };
 
 // Named barrier over one warpgroup that also ORs a flag across it.
@@ -141,13 +168,14 @@ struct Ring {
   }
 };
 
-constexpr int kTmaRegs = 64;
 
 // FP64-pipe rows j0 .. j0+3 (warps 0-3): HwCol's weighted sum from staged
 // tiles.  Returns true if a wait ran out.
-__device__ __forceinline__ bool hw_rows(const Maps &maps, SmemT &sm, double *__restrict__ un,
-                                        int i, int j, int nx, int ny, int P, size_t S, int kb,
-                                        int ke, unsigned wait_limit) {
+template <bool RHS>
+__device__ __forceinline__ bool hw_rows(const Maps &maps, SmemT<RHS> &sm,
+                                        double *__restrict__ un, int i, int j, int nx, int ny,
+                                        int P, size_t S, int kb, int ke, unsigned wait_limit) {
+  typedef HwSlotT<RHS> HwSlot;
   const int t = threadIdx.x + 32 * threadIdx.y;                  // 0 .. 127
   const int ou = (threadIdx.y + 1) * RW + threadIdx.x + 1;       // u, cy: box rows from j0 - 1
   const int ow = threadIdx.y * RW + threadIdx.x + 1;             // c0, cx, cz: box rows from j0
@@ -167,12 +195,13 @@ __device__ __forceinline__ bool hw_rows(const Maps &maps, SmemT &sm, double *__r
     HwSlot &sl = sm.hw[s];
     u64 *b = &sm.hbar[s];
     tma::fence_proxy_async();
-    tma::mbar_expect(b, kHwSlotBytes);
+    tma::mbar_expect(b, kHwSlotBytes<RHS>);
     tma::load3(sl.u, &maps.u, X0, YU, p, b);
     tma::load3(sl.c0, &maps.c0, X0, YW, p, b);
     tma::load3(sl.cx, &maps.cx, X0, YW, p, b);
     tma::load3(sl.cz, &maps.cz, X0, YW, p, b);
     tma::load3(sl.cy, &maps.cy, X0, YU, p, b);
+    if constexpr (RHS) tma::load3(sl.r, &maps.r, X0, YW, p, b);
   };
   for (int p = kb - 1; p <= kb + 2; ++p) issue(p);
   bool failed = false;
@@ -201,7 +230,11 @@ __device__ __forceinline__ bool hw_rows(const Maps &maps, SmemT &sm, double *__r
     const double wu = sk.cz[ow];
     if (active) {
       // HwCol::step's operation order (bit-identical results)
-      double acc = sk.c0[ow] * uc;
+      double acc;
+      if constexpr (RHS)
+        acc = fma(sk.c0[ow], uc, sk.r[ow]);
+      else
+        acc = sk.c0[ow] * uc;
       acc = fma(sk.cx[ow], sk.u[ou + 1], acc);
       acc = fma(sk.cx[ow - 1], sk.u[ou - 1], acc);
       acc = fma(sk.cy[ou], sk.u[ou + RW], acc);
@@ -220,9 +253,11 @@ __device__ __forceinline__ bool hw_rows(const Maps &maps, SmemT &sm, double *__r
 
 // Integer rows j0+4 .. j0+7 (warps 4-7): walk::int_point from decoded tiles.
 // Returns true if a wait ran out.
-__device__ __forceinline__ bool int_rows(const Maps &maps, SmemT &sm, double *__restrict__ un,
-                                         int i, int j, int nx, int ny, int P, size_t S, int kb,
-                                         int ke, unsigned wait_limit) {
+template <bool RHS>
+__device__ __forceinline__ bool int_rows(const Maps &maps, SmemT<RHS> &sm,
+                                         double *__restrict__ un, int i, int j, int nx, int ny,
+                                         int P, size_t S, int kb, int ke, unsigned wait_limit) {
+  typedef IntSlotT<RHS> IntSlot;
   const int t = threadIdx.x + 32 * (threadIdx.y - 4);        // 0 .. 127
   const int own = (threadIdx.y - 3) * RW + threadIdx.x + 1;  // box rows 1..4, columns 1..32
   const bool active = i < nx - 1 && j < ny - 1;
@@ -249,9 +284,10 @@ __device__ __forceinline__ bool int_rows(const Maps &maps, SmemT &sm, double *__
     IntSlot &sl = sm.in[s];
     u64 *b = &sm.ibar[s];
     tma::fence_proxy_async();
-    tma::mbar_expect(b, kIntSlotBytes);
+    tma::mbar_expect(b, kIntSlotBytes<RHS>);
     tma::load3(sl.u, &maps.u, X0, Y0, p, b);
     tma::load3(sl.k, &maps.k, X0, Y0, p, b);
+    if constexpr (RHS) tma::load3(sl.r, &maps.r, X0, Y0 + 1, p, b);  // own rows only
   };
   // Decode plane p of the ring into decoded slot d; returns this thread's own
   // column value (raw bits and decoded).
@@ -314,9 +350,11 @@ __device__ __forceinline__ bool int_rows(const Maps &maps, SmemT &sm, double *__
       const walk::Dec dn{ek[own + RW], mk[own + RW]}, ds{ek[own - RW], mk[own - RW]};
       const u64 Ku = sm.in[(k + 1) & (NR - 1)].k[own];
       const u64 bcc = bc, bdd = bd, buu = bu;
-      un[c] = walk::int_point<false>(
+      u64 br = 0ull;
+      if constexpr (RHS) br = rk.r[own - RW];  // the source box starts at box row 1
+      un[c] = walk::int_point<RHS>(
           dc, du, dd, de, dw, dn, ds, Kc, Ku, Kd, rk.k[own + 1], rk.k[own - 1], rk.k[own + RW],
-          rk.k[own - RW], 0ull, [&] {
+          rk.k[own - RW], br, [&] {
             return walk::Raw7{bcc, rk.u[own + 1], rk.u[own - 1], rk.u[own + RW], rk.u[own - RW],
                               buu, bdd};
           });
@@ -332,15 +370,15 @@ __device__ __forceinline__ bool int_rows(const Maps &maps, SmemT &sm, double *__
   return failed;
 }
 
-template <int REGS = kTmaRegs>
-__global__ void __launch_bounds__(TX *TY, 4)
+template <bool RHS, int MINB, int REGS>
+__global__ void __launch_bounds__(TX *TY, MINB)
     k_fast_tma(const __grid_constant__ Maps maps, double *__restrict__ un, int nx, int ny,
                int nz, int P, size_t S, int kchunk, int *__restrict__ err, unsigned wait_limit) {
   const int kb = 1 + blockIdx.z * kchunk;
   const int ke = min(kb + kchunk, nz - 1);
   if (kb >= ke) return;  // whole block
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  SmemT &sm = *reinterpret_cast<SmemT *>(smem_raw);
+  SmemT<RHS> &sm = *reinterpret_cast<SmemT<RHS> *>(smem_raw);
   const int i = 1 + blockIdx.x * TX + threadIdx.x;
   const int j = 1 + blockIdx.y * TY + threadIdx.y;
   bool failed;
@@ -356,48 +394,72 @@ __global__ void __launch_bounds__(TX *TY, 4)
   if (failed && (threadIdx.x | (threadIdx.y & 3)) == 0) atomicExch(err, 1);
 }
 
-size_t tma_smem() { return sizeof(SmemT) + 128; }
+// Launch shape per variant: without a source term 4 blocks per SM at 64
+// registers (47 KB of shared memory each); with one 3 blocks per SM at 80
+// registers (56 KB: the source boxes would not fit four).
+template <bool RHS>
+struct Variant {
+  static constexpr int kMinb = RHS ? 3 : 4;
+  static constexpr int kRegs = RHS ? 80 : 64;
+  static size_t smem() { return sizeof(SmemT<RHS>) + 128; }
+  static auto kernel() { return k_fast_tma<RHS, kMinb, kRegs>; }
+  // The kernel compiled to the register count its setmaxnreg counts assume.
+  static bool usable() {
+    static const bool ok = [] {
+      if (!tma::encoder()) return false;
+      cudaFuncAttributes a;
+      if (cudaFuncGetAttributes(&a, kernel()) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+      }
+      if (a.numRegs != kRegs) return false;
+      return cudaFuncSetAttribute(kernel(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem()) == cudaSuccess;
+    }();
+    return ok;
+  }
+};
 
 bool encode_f64(CUtensorMap *m, const void *base, const heat_geom &g, unsigned rows) {
   return tma::encode_field(m, base, CU_TENSOR_MAP_DATA_TYPE_UINT64, 8, g, RW, rows);
+}
+
+template <bool RHS>
+cudaError_t launch_variant(const Maps &m, double *u_new, const heat_geom &g, int *err,
+                           cudaStream_t st, unsigned wait_limit) {
+  typedef Variant<RHS> V;
+  static const long resident = resident_blocks((const void *)V::kernel(), TX * TY, V::smem());
+  const int kc = wave_chunk(g, TX, TY, resident);
+  dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
+  V::kernel()<<<gr, dim3(TX, TY), V::smem(), st>>>(m, u_new, g.nx, g.ny, g.nz, g.pitch, g.plane,
+                                                   kc, err, wait_limit);
+  return cudaGetLastError();
 }
 
 }  // namespace
 
 // Usable when the tensor-map encoder is available, the field rows are
 // multiples of 16 bytes (pitch a multiple of 2 points: always, it is a
-// multiple of 4) and the kernel compiled to the register count its setmaxnreg
-// bounds assume.
-bool fast_tma_usable(const heat_geom &g) {
-  static const bool ok = [] {
-    if (!tma::encoder()) return false;
-    cudaFuncAttributes a;
-    if (cudaFuncGetAttributes(&a, k_fast_tma<>) != cudaSuccess) {
-      cudaGetLastError();
-      return false;
-    }
-    if (a.numRegs != kTmaRegs) return false;
-    return cudaFuncSetAttribute(k_fast_tma<>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tma_smem()) == cudaSuccess;
-  }();
+// multiple of 4) and the variant compiled to the register count its setmaxnreg
+// counts assume.
+bool fast_tma_usable(const heat_geom &g, bool rhs) {
+  const bool ok = rhs ? Variant<true>::usable() : Variant<false>::usable();
   return ok && (g.pitch % 2) == 0;
 }
 
 cudaError_t launch_fast_tma(double *u_new, const double *u_old, const unsigned long long *K,
-                            const double *c0, double *const cf[3], const heat_geom &g, int *err,
-                            cudaStream_t st, unsigned wait_limit) {
+                            const double *c0, double *const cf[3], const double *rhs,
+                            const heat_geom &g, int *err, cudaStream_t st, unsigned wait_limit) {
   Maps m;
   if (!encode_f64(&m.u, u_old, g, 6) || !encode_f64(&m.k, K, g, 6) ||
       !encode_f64(&m.c0, c0, g, 4) || !encode_f64(&m.cx, cf[0], g, 4) ||
-      !encode_f64(&m.cz, cf[2], g, 4) || !encode_f64(&m.cy, cf[1], g, 5))
+      !encode_f64(&m.cz, cf[2], g, 4) || !encode_f64(&m.cy, cf[1], g, 5) ||
+      (rhs && !encode_f64(&m.r, rhs, g, 4)))
     return cudaErrorInvalidValue;
+  if (!rhs) std::memset(&m.r, 0, sizeof m.r);
   if (wait_limit > tma::kWaitLimit) wait_limit = tma::kWaitLimit;
-  static const long resident = resident_blocks((const void *)k_fast_tma<>, TX * TY, tma_smem());
-  const int kc = wave_chunk(g, TX, TY, resident);
-  dim3 gr((g.nx - 2 + TX - 1) / TX, (g.ny - 2 + TY - 1) / TY, (g.nz - 2 + kc - 1) / kc);
-  k_fast_tma<><<<gr, dim3(TX, TY), tma_smem(), st>>>(m, u_new, g.nx, g.ny, g.nz, g.pitch,
-                                                     g.plane, kc, err, wait_limit);
-  return cudaGetLastError();
+  return rhs ? launch_variant<true>(m, u_new, g, err, st, wait_limit)
+             : launch_variant<false>(m, u_new, g, err, st, wait_limit);
 }
 
 }  // namespace heat

@@ -163,12 +163,13 @@ cudaError_t launch_fast_mix(double *u_new, const double *u_old, const double *rh
                             double *const cf[3], const heat_geom &g, int hw_rows,
                             int *err, cudaStream_t st);
 
-// heat_fp64_tma.cu: the hw_rows = 4, no-source-term split with the integer
-// rows' plane tiles staged by TMA (bit-identical to the k_fast_ws launch).
-bool fast_tma_usable(const heat_geom &g);
+// heat_fp64_tma.cu: the hw_rows = 4 split with every input staged by TMA
+// (bit-identical to the k_fast_ws launch), with or without a source term.
+bool fast_tma_usable(const heat_geom &g, bool rhs = false);
 cudaError_t launch_fast_tma(double *u_new, const double *u_old, const unsigned long long *K,
-                            const double *c0, double *const cf[3], const heat_geom &g, int *err,
-                            cudaStream_t st, unsigned wait_limit = kWaitLimit);
+                            const double *c0, double *const cf[3], const double *rhs,
+                            const heat_geom &g, int *err, cudaStream_t st,
+                            unsigned wait_limit = kWaitLimit);
 // n steps of context c from buffer `cur` on stream st with its own
 // single-grid kernels (two steps per launch where its form has them); the
 // context's bookkeeping is untouched.  ctx_flips gives the parity of buffer

@@ -135,6 +135,20 @@ def test_default_fp64_kernel_timeout(H, oracle):
     with H.Solver(kappa, u0, h, dt) as ref:
         ref.step(7)
         assert bits_equal(got, ref.field())
+    # the same launch with a source term (the reference problem)
+    kappa, rhs, u0, h, dt = H.inputs_reference(40)
+    with H.Solver(kappa, u0, h, dt, rhs=rhs) as s:
+        s.step(2)
+        before = s.field()
+        assert lib.heat_diag_fp64_timeout(s._ctx) == H.HEAT_OK
+        out = np.empty_like(before)
+        assert lib.heat_get_field(s._ctx, out.ctypes.data) == H.HEAT_ETIMEOUT
+        assert bits_equal(out, before)
+        s.step(3)
+        got = s.field()
+    with H.Solver(kappa, u0, h, dt, rhs=rhs) as ref:
+        ref.step(5)
+        assert bits_equal(got, ref.field())
     with H.Solver(kappa, u0, h, dt, flags=H.HEAT_BITEXACT) as s:
         assert H.lib().heat_diag_fp64_timeout(s._ctx) == H.HEAT_ESTATE
     assert small_solve_matches_oracle(H, oracle)
