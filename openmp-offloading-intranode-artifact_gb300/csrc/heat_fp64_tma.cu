@@ -1,6 +1,7 @@
-// Default FP64 form, no source term: the warpgroup-split launch with every
-// input staged in shared memory by TMA and every integer-row value decoded
-// once.
+// Default FP64 form: the warpgroup-split launch with every input staged in
+// shared memory by TMA and every integer-row value decoded once, with or
+// without a source term (then a 34 x 4 box of it per slot at each
+// warpgroup's own rows, 3 blocks per SM at 80 registers instead of 4 at 64).
 //
 // Same split and the same arithmetic as k_fast_ws (heat_fp64_int.cu): blocks of
 // 32 x 8 columns walk a z-chunk; warps 0-3 evaluate the FP64-pipe rows
